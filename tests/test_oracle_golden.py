@@ -1,0 +1,112 @@
+"""Pin the CPU oracle (oracle/ceed_oracle.c) to vectors produced by the reference libCEED.
+
+The fixtures in tests/golden/ come from the reference's own `/cpu/self/ref/serial`
+backend driven through the libCEED API (tests/golden/make_golden.py).  These tests
+need no GPU.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from tests.conftest import GOLDEN, relinf
+
+CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f != "basis.npz")
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _problem(case):
+    kind, n, p = case.split("_")
+    n, p = int(n[1:]), int(p[1:])
+    seeds = {"mass": 1001, "poisson": 2000 + p, "vpoisson": 3000 + p, "vmass": 3100 + p, "kappa": 4000 + p}
+    noise = 0.1 if kind == "mass" else 0.05
+    return orc.BoxProblem(n, p, ncomp=3 if kind.startswith("v") else 1, poisson=kind not in ("mass", "vmass"), noise=noise,
+                          seed=seeds[kind], kappa=kind == "kappa")
+
+
+@pytest.fixture(scope="module")
+def basis_gold():
+    return np.load(os.path.join(GOLDEN, "basis.npz"))
+
+
+@pytest.mark.parametrize("P", range(2, 11))
+def test_basis_tables_match_reference(basis_gold, P):
+    Q = P + 1
+    interp, grad, qref, qw = orc.lagrange_1d(P, Q, orc.GAUSS)
+    tag = f"basis_P{P}_Q{Q}_gauss_"
+    # Same recurrences as the reference: bitwise equal.
+    assert np.array_equal(interp.ravel(), basis_gold[tag + "interp"])
+    assert np.array_equal(grad.ravel(), basis_gold[tag + "grad"])
+    assert np.array_equal(qref, basis_gold[tag + "qref"])
+    assert np.array_equal(qw, basis_gold[tag + "qweight"])
+    # Collocated gradient through a different pseudoinverse: equal to rounding.
+    colo = orc.collocated_grad(P, Q, interp, grad)
+    assert np.max(np.abs(colo.ravel() - basis_gold[tag + "colograd"])) < 1e-11 * max(1.0, np.max(np.abs(colo)))
+
+
+def test_lobatto_tables_match_reference(basis_gold):
+    interp, grad, qref, qw = orc.lagrange_1d(4, 4, orc.GAUSS_LOBATTO)
+    assert np.array_equal(qref, basis_gold["basis_P4_Q4_lobatto_qref"])
+    assert np.array_equal(qw, basis_gold["basis_P4_Q4_lobatto_qweight"])
+    assert np.allclose(interp.ravel(), basis_gold["basis_P4_Q4_lobatto_interp"], atol=1e-15)
+    assert np.allclose(grad.ravel(), basis_gold["basis_P4_Q4_lobatto_grad"], atol=1e-13)
+
+
+@pytest.mark.parametrize("mode", ["interp", "grad"])
+def test_basis_apply_matches_reference(basis_gold, mode):
+    P, Q, nc = 4, 5, 2
+    interp, grad, qref, qw = orc.lagrange_1d(P, Q)
+    em = orc.EVAL_INTERP if mode == "interp" else orc.EVAL_GRAD
+    u = orc.fill_uniform(100 + (mode == "grad"), P ** 3 * nc)
+    ut = orc.fill_uniform(200 + (mode == "grad"), Q ** 3 * nc * (3 if mode == "grad" else 1))
+    assert np.array_equal(u, basis_gold[f"bapply_{mode}_u"])
+    v = orc.basis_apply(3, P, Q, nc, interp, grad, qw, 1, orc.NOTRANSPOSE, em, u)
+    vt = orc.basis_apply(3, P, Q, nc, interp, grad, qw, 1, orc.TRANSPOSE, em, ut)
+    assert relinf(v, basis_gold[f"bapply_{mode}_v"]) < 1e-13
+    assert relinf(vt, basis_gold[f"bapply_{mode}_vt"]) < 1e-13
+    w = orc.basis_apply(3, P, Q, 1, interp, grad, qw, 1, orc.NOTRANSPOSE, orc.EVAL_WEIGHT, None)
+    assert np.array_equal(w, basis_gold["bapply_weight"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_operator_matches_reference(case):
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    pb = _problem(case)
+    # Inputs regenerate bit-for-bit.
+    assert _sha(pb.coords) == str(g["sha_coords"])
+    assert _sha(pb.offsets) == str(g["sha_offsets"])
+    assert _sha(pb.u) == str(g["sha_u"])
+    # Geometric factors from the gallery build QFunction: same arithmetic, equal to rounding.
+    assert relinf(pb.qdata, g["qdata"]) < 1e-13
+    # Operator apply: within 1e-12 relative l-infinity (measured ~1e-15).
+    if "kappa" in g:
+        pb.kappa = g["kappa"]
+    v = pb.apply()
+    assert relinf(v, g["v"]) < 1e-12
+    if "egather" in g:
+        e = orc.rstr_gather(pb.offsets, pb.P ** 3, pb.ncomp, pb.comp_stride, pb.u)
+        assert np.array_equal(e, g["egather"])  # gathers are bit-exact
+        l = orc.rstr_scatter_add(pb.offsets, pb.P ** 3, pb.ncomp, pb.comp_stride, e, np.zeros(pb.l_size))
+        assert np.array_equal(l, g["escatter"])  # element-order scatter: bit-exact
+    if "kgrad" in g:
+        # kappa = exp(g) is stored: libm exp may differ in the last bit across hosts.
+        assert np.max(np.abs(pb.kappa - g["kappa"])) < 1e-15 * np.max(g["kappa"])
+        pb.kappa = g["kappa"]
+        assert relinf(pb.apply(), g["v"]) < 1e-12
+        f = orc.fill_uniform(4003 + 3, pb.l_size)
+        assert _sha(f) == str(g["sha_f"])
+        w = pb.apply() - f
+        kg = orc.kappa_grad(pb.P, pb.Q, pb.offsets, pb.l_size, pb.interp, pb.grad, pb.qdata, pb.u, w)
+        assert relinf(kg, g["kgrad"]) < 1e-12
+
+
+def test_poisson_constant_nullspace():
+    """A 1 = 0 for the diffusion operator (the reference's t522 check), on the oracle."""
+    pb = orc.BoxProblem(3, 4, poisson=True, seed=7)
+    v = pb.apply(np.ones(pb.l_size))
+    assert np.max(np.abs(v)) < 1e-13
