@@ -1,0 +1,177 @@
+/*
+ * libceed_b200: the C ABI of the GB300 (sm_103a) operator-apply backend.
+ *
+ * These are the entry points that the libCEED backend `/gpu/cuda/b200` (host code in C, see
+ * libceed_gb300/backend/) binds: plain pointers, sizes and POD descriptors, an `int` status on every
+ * call (0 = success), and no CPU fallback.  Each entry point names the reference interface whose
+ * work it takes over.  References are paths inside the libCEED source tree.
+ *
+ * Data layouts chosen by this backend (published to libCEED through CeedElemRestrictionSetELayout):
+ *   L-vector   component k of the node at offset o lives at o + k*comp_stride
+ *   E-vector   [comp][elem][node]   (ELayout {1, num_elem*elem_size, elem_size})
+ *   Q-vector   [eval-dim][comp][elem][qpt]
+ *   qdata      strided E-vector with backend strides: [comp][elem][qpt]
+ *   offsets    int32 [elem][node], device memory
+ *   1D matrices row-major Q x P (interp, grad) and Q x Q (collocated grad), host memory at create time
+ *
+ * Precision: B200_F64 kernels compute in double; B200_F32 kernels compute and accumulate in float.
+ * Every call is asynchronous on the context's stream unless it returns a host value.
+ */
+#ifndef CEED_B200_H
+#define CEED_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes mirror include/ceed/types.h CeedErrorType. */
+enum {
+  B200_SUCCESS            = 0,
+  B200_ERROR_MINOR        = 1,
+  B200_ERROR_DIMENSION    = 2,
+  B200_ERROR_INCOMPLETE   = 3,
+  B200_ERROR_INCOMPATIBLE = 4,
+  B200_ERROR_ACCESS       = 5,
+  B200_ERROR_UNSUPPORTED  = -2,
+  B200_ERROR_BACKEND      = -1,
+};
+
+enum { B200_F64 = 0, B200_F32 = 1 };
+enum { B200_NOTRANSPOSE = 0, B200_TRANSPOSE = 1 };                                             /* CeedTransposeMode */
+enum { B200_EVAL_NONE = 0, B200_EVAL_INTERP = 1, B200_EVAL_GRAD = 2, B200_EVAL_WEIGHT = 16 }; /* CeedEvalMode */
+enum { B200_NORM_1 = 0, B200_NORM_2 = 1, B200_NORM_MAX = 2 };                                  /* CeedNormType */
+enum { B200_COPY_H2D = 1, B200_COPY_D2H = 2, B200_COPY_D2D = 3 };
+enum { B200_SCATTER_ATOMIC = 0, B200_SCATTER_DETERMINISTIC = 1 };
+
+/* Pointwise kernels of the fused operator: the gallery QFunctions of the path
+ * (include/ceed/jit-source/gallery/ *.h) plus the kappa-weighted diffusion. */
+enum {
+  B200_QF_MASS           = 0, /* MassApply:             u, qdata(1)            -> v      */
+  B200_QF_POISSON        = 1, /* Poisson3DApply:        du, qdata(6)           -> dv     */
+  B200_QF_VECMASS        = 2, /* Vector3MassApply:      u(3), qdata(1)         -> v(3)   */
+  B200_QF_VECPOISSON     = 3, /* Vector3Poisson3DApply: du(3), qdata(6)        -> dv(3)  */
+  B200_QF_POISSON_KAPPA  = 4, /* Poisson3DApply with qdata scaled by kappa[elem][qpt]     */
+};
+
+typedef struct b200_ctx_s   *b200_ctx;
+typedef struct b200_basis_s *b200_basis;
+typedef struct b200_plan_s  *b200_plan;
+typedef struct b200_op_s    *b200_op;
+
+/* Message of the last failing call on this thread. */
+const char *b200_last_error(void);
+
+/* ---- Context: one per Ceed.  Replaces CeedInit_Cuda device selection (backends/cuda/ceed-cuda-common.c:19-35)
+ *      and CeedSetStream (interface/ceed.c:1408). ---------------------------------------------------------------- */
+int b200_ctx_create(int device_id, b200_ctx *ctx);
+int b200_ctx_set_stream(b200_ctx ctx, void *cuda_stream);
+int b200_ctx_get_stream(b200_ctx ctx, void **cuda_stream);
+int b200_ctx_sync(b200_ctx ctx);
+int b200_ctx_destroy(b200_ctx ctx);
+/* Number of kernels this library launched on the context (all entry points). */
+int b200_ctx_launch_count(b200_ctx ctx, int64_t *count);
+
+/* ---- Device memory of CeedVector arrays.  Replaces the device half of CeedVectorCreate_Cuda / SetArray /
+ *      SyncArray (backends/cuda-ref/ceed-cuda-ref-vector.c:97-262). ------------------------------------------------ */
+int b200_alloc(b200_ctx ctx, size_t bytes, void **dptr);
+int b200_free(b200_ctx ctx, void *dptr);
+int b200_copy(b200_ctx ctx, void *dst, const void *src, size_t bytes, int kind);
+
+/* ---- Vector BLAS-1.  Replaces backends/cuda-ref/kernels/cuda-ref-vector.cu:14-220 and the cuBLAS norm calls of
+ *      backends/cuda-ref/ceed-cuda-ref-vector.c:487-640 (CeedVectorSetValue/Scale/AXPY/AXPBY/PointwiseMult/
+ *      Reciprocal/Norm, interface/ceed-vector.c:377-953).  b200_vec_dot has no CeedVector counterpart (the CG
+ *      driver needs it); b200_vec_convert copies between precisions. -------------------------------------------- */
+int b200_vec_set_value(b200_ctx ctx, int prec, int64_t n, void *x, double value);
+int b200_vec_scale(b200_ctx ctx, int prec, int64_t n, void *x, double alpha);
+int b200_vec_axpy(b200_ctx ctx, int prec, int64_t n, double alpha, const void *x, void *y);
+int b200_vec_axpby(b200_ctx ctx, int prec, int64_t n, double alpha, double beta, const void *x, void *y);
+int b200_vec_pointwise_mult(b200_ctx ctx, int prec, int64_t n, void *w, const void *x, const void *y);
+int b200_vec_reciprocal(b200_ctx ctx, int prec, int64_t n, void *x);
+int b200_vec_norm(b200_ctx ctx, int prec, int64_t n, const void *x, int norm_type, double *norm);
+int b200_vec_dot(b200_ctx ctx, int prec, int64_t n, const void *x, const void *y, double *dot);
+int b200_vec_convert(b200_ctx ctx, int64_t n, int src_prec, const void *src, int dst_prec, void *dst);
+
+/* ---- Element restriction.  Offset form replaces OffsetNoTranspose / OffsetTranspose
+ *      (include/ceed/jit-source/cuda/cuda-ref-restriction-offset.h:15-67, host side
+ *      backends/cuda-ref/ceed-cuda-ref-restriction.c); strided form replaces cuda-ref-restriction-strided.h.
+ *      Gather: e = E l (bit-exact copy).  Scatter: l += E^T e, atomic (any order) or deterministic (fixed
+ *      per-node order from the inverse-offset plan, bit-reproducible run to run). ------------------------------- */
+int b200_rstr_gather(b200_ctx ctx, int prec, int64_t num_elem, int elem_size, int num_comp, int64_t comp_stride, int64_t l_size,
+                     const int32_t *offsets, const void *l_vec, void *e_vec);
+int b200_rstr_scatter_atomic(b200_ctx ctx, int prec, int64_t num_elem, int elem_size, int num_comp, int64_t comp_stride, int64_t l_size,
+                             const int32_t *offsets, const void *e_vec, void *l_vec);
+/* Inverse-offset plan for the deterministic scatter: replaces the host CSR build of
+ * backends/cuda-ref/ceed-cuda-ref-restriction.c:416-493.  offsets_host may be NULL when offsets_dev is given. */
+int b200_plan_create(b200_ctx ctx, int64_t num_elem, int elem_size, int num_comp, int64_t comp_stride, int64_t l_size,
+                     const int32_t *offsets_host, const int32_t *offsets_dev, b200_plan *plan);
+int b200_plan_destroy(b200_plan plan);
+/* l = E^T e (add = 0; entries the restriction does not reach become 0) or l += E^T e (add = 1), summing each node's
+ * entries in ascending E-index order. */
+int b200_rstr_scatter_det(b200_ctx ctx, b200_plan plan, int prec, const void *e_vec, void *l_vec, int add);
+int b200_rstr_strided_gather(b200_ctx ctx, int prec, int64_t num_elem, int elem_size, int num_comp, const int64_t strides[3],
+                             const void *l_vec, void *e_vec);
+int b200_rstr_strided_scatter(b200_ctx ctx, int prec, int64_t num_elem, int elem_size, int num_comp, const int64_t strides[3],
+                              const void *e_vec, void *l_vec);
+
+/* ---- Tensor H1 basis (dim 1..3, P, Q <= 16).  Replaces CeedBasisCreateTensorH1_Cuda and the Interp/Grad/Weight
+ *      kernels of include/ceed/jit-source/cuda/cuda-ref-basis-tensor.h (CeedBasisApply / ApplyAdd,
+ *      interface/ceed-basis.c:2083-2111).  add = 1 accumulates into v (TRANSPOSE only, as ApplyAdd). ------------ */
+int b200_basis_create(b200_ctx ctx, int dim, int P_1d, int Q_1d, int num_comp, const double *interp_1d, const double *grad_1d,
+                      const double *q_weight_1d, b200_basis *basis);
+int b200_basis_apply(b200_basis basis, int prec, int64_t num_elem, int t_mode, int eval_mode, int add, const void *u, void *v);
+int b200_basis_destroy(b200_basis basis);
+
+/* ---- Gallery QFunctions on Q-vectors (unfused path).  Replaces CeedQFunctionApply_Cuda with the JIT'd gallery
+ *      sources (backends/cuda-ref/ceed-cuda-ref-qfunction.c).  in/out are arrays of device pointers in the order of
+ *      the gallery field lists; kappa-weighted diffusion takes (du, qdata, kappa). ------------------------------ */
+int b200_qf_apply(b200_ctx ctx, int prec, int qf_kind, int64_t num_points, const void *const *in, void *const *out);
+
+/* ---- Geometric factors.  Replaces the setup operator with gallery Mass3DBuild / Poisson3DBuild
+ *      (include/ceed/jit-source/gallery/ceed-mass3dbuild.h, ceed-poisson3dbuild.h) on a trilinear coordinate field:
+ *      coords has 3 components at comp_stride, x_offsets are [elem][8] vertex offsets.  qdata (FP64) is written in
+ *      the backend layout [comp][elem][qpt] with 1 (mass) or 6 (Poisson, Voigt order) components. ------------- */
+int b200_qdata_build(b200_ctx ctx, int poisson, int64_t num_elem, int Q_1d, const double *x_interp_1d, const double *x_grad_1d,
+                     const double *q_weight_1d, const int32_t *x_offsets, int64_t x_comp_stride, const double *coords, double *qdata);
+
+/* ---- Fused operator apply (the hot path).  Replaces CeedOperatorApplyAdd_Cuda_gen and its generated kernel
+ *      (backends/cuda-gen/ceed-cuda-gen-operator.c:105-300, ceed-cuda-gen-operator-build.cpp:1158-1680) and the
+ *      ref backend's element loop (backends/ref/ceed-ref-operator.c:381-476): gather -> interp/grad -> pointwise
+ *      kernel -> transposes -> scatter in one kernel per element batch. -------------------------------------------- */
+typedef struct {
+  int            qf;          /* B200_QF_* */
+  int            prec;        /* B200_F64 or B200_F32 */
+  int            P_1d, Q_1d;  /* Q_1d = P_1d + 1 for the compiled kernels, P_1d in 2..9 */
+  int            num_comp;    /* 1, or 3 for the vector QFunctions */
+  int            scatter;     /* B200_SCATTER_ATOMIC or B200_SCATTER_DETERMINISTIC */
+  int64_t        num_elem;
+  int64_t        l_size;      /* length of u and v */
+  int64_t        comp_stride; /* component stride of the L-vector */
+  const int32_t *offsets;     /* device, [elem][P^3] */
+  const double  *interp_1d;   /* host, Q x P */
+  const double  *grad_1d;     /* host, Q x P */
+  int            elems_per_block; /* 0: tuned default */
+  int            staging;         /* 0: default, 1: registers, 2: shared memory */
+} b200_op_desc;
+
+int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);
+/* v = A u (add = 0, CeedOperatorApply) or v += A u (add = 1, CeedOperatorApplyAdd).  qdata: [comp][elem][qpt] in
+ * the operator's precision; kappa: [elem][qpt] or NULL. */
+int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add);
+/* Algorithmic bytes and FLOPs of one apply (for roofline reporting). */
+int b200_op_cost(b200_op op, double *bytes, double *flops);
+/* Launch shape in use: elements per block and threads per block. */
+int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_per_block, int *staging);
+int b200_op_set_tile(b200_op op, int elems_per_block, int staging);
+int b200_op_destroy(b200_op op);
+
+/* Adjoint of the kappa-weighted diffusion with respect to kappa: g[elem][qpt] = grad(w) . D grad(u), recomputing the
+ * gradients from u and w (no stored E-vectors).  Both in the operator's precision. */
+int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qdata, void *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

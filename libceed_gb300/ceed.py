@@ -1,0 +1,480 @@
+"""Python face of the `/gpu/cuda/b200` backend, mirroring libCEED's Python binding.
+
+Names, arguments and behaviour follow python/ceed.py, ceed_vector.py, ceed_elemrestriction.py,
+ceed_basis.py, ceed_qfunction.py and ceed_operator.py of the reference, so code written against
+`libceed.Ceed("/gpu/cuda/...")` reads the same here.  Every compute call goes through the C ABI of
+libceed_b200.so (include/ceed-b200.h); device memory and the stream come from PyTorch.  There is no
+CPU fallback: a missing library or an unsupported configuration raises.
+
+Layouts (published the way CeedElemRestrictionSetELayout does):
+  E-vector [comp][elem][node], Q-vector [eval-dim][comp][elem][qpt], qdata [comp][elem][qpt].
+"""
+import ctypes
+import re
+
+import numpy as np
+import torch
+
+from . import basis1d
+from ._ffi import B200Error, OpDesc, call, load
+
+# Constants of include/ceed/ceed.h
+MEM_HOST, MEM_DEVICE = 0, 1
+COPY_VALUES, USE_POINTER, OWN_POINTER = 0, 1, 2
+NOTRANSPOSE, TRANSPOSE = 0, 1
+EVAL_NONE, EVAL_INTERP, EVAL_GRAD, EVAL_DIV, EVAL_CURL, EVAL_WEIGHT = 0, 1, 2, 4, 8, 16
+NORM_1, NORM_2, NORM_MAX = 0, 1, 2
+GAUSS, GAUSS_LOBATTO = basis1d.GAUSS, basis1d.GAUSS_LOBATTO
+REQUEST_IMMEDIATE = None
+STRIDES_BACKEND = "backend"
+SCATTER_ATOMIC, SCATTER_DETERMINISTIC = 0, 1
+F64, F32 = 0, 1
+
+# Gallery QFunctions on the hot path (include/ceed/jit-source/gallery/*.h), plus the kappa-weighted diffusion
+# this backend adds for the differentiable operator.  Fields: (name, size, eval mode).
+QF_MASS, QF_POISSON, QF_VECMASS, QF_VECPOISSON, QF_POISSON_KAPPA = 0, 1, 2, 3, 4
+GALLERY = {
+    "MassApply": (QF_MASS, [("u", 1, EVAL_INTERP), ("qdata", 1, EVAL_NONE)], [("v", 1, EVAL_INTERP)]),
+    "Poisson3DApply": (QF_POISSON, [("du", 3, EVAL_GRAD), ("qdata", 6, EVAL_NONE)], [("dv", 3, EVAL_GRAD)]),
+    "Vector3MassApply": (QF_VECMASS, [("u", 3, EVAL_INTERP), ("qdata", 1, EVAL_NONE)], [("v", 3, EVAL_INTERP)]),
+    "Vector3Poisson3DApply": (QF_VECPOISSON, [("du", 9, EVAL_GRAD), ("qdata", 6, EVAL_NONE)], [("dv", 9, EVAL_GRAD)]),
+    "Poisson3DApplyKappa": (QF_POISSON_KAPPA, [("du", 3, EVAL_GRAD), ("qdata", 6, EVAL_NONE), ("kappa", 1, EVAL_NONE)],
+                            [("dv", 3, EVAL_GRAD)]),
+    "Mass3DBuild": ("build_mass", [("dx", 9, EVAL_GRAD), ("weights", 1, EVAL_WEIGHT)], [("qdata", 1, EVAL_NONE)]),
+    "Poisson3DBuild": ("build_poisson", [("dx", 9, EVAL_GRAD), ("weights", 1, EVAL_WEIGHT)], [("qdata", 6, EVAL_NONE)]),
+}
+
+
+def _vp(x):
+    return ctypes.c_void_p(x)
+
+
+class Ceed:
+    """A device context of the `/gpu/cuda/b200` backend (resource string `/gpu/cuda/b200[:device_id=N]`)."""
+
+    def __init__(self, resource="/gpu/cuda/b200", on_error="store", deterministic=False):
+        m = re.match(r"^/gpu/cuda/b200(?::device_id=(\d+))?$", resource)
+        if not m:
+            raise B200Error("CeedInit", 1, f"resource {resource!r} is not /gpu/cuda/b200[:device_id=N]")
+        if not torch.cuda.is_available():
+            raise B200Error("CeedInit", -1, "/gpu/cuda/b200 needs a CUDA device; none is visible")
+        self.device_id = int(m.group(1) or 0)
+        self.resource = resource
+        self.device = torch.device("cuda", self.device_id)
+        load()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            call("b200_ctx_create", self.device_id, ctypes.byref(h))
+        self._ctx = h
+        self.deterministic = deterministic
+        self.set_stream(torch.cuda.current_stream(self.device))
+
+    # ---- libCEED Ceed methods -------------------------------------------------------------------------------------
+    def get_resource(self):
+        return self.resource
+
+    def get_preferred_memtype(self):
+        return MEM_DEVICE
+
+    def set_deterministic(self, flag=True):
+        """CeedSetDeterministic: transposed restrictions and operators use the inverse-offset scatter."""
+        self.deterministic = bool(flag)
+
+    def is_deterministic(self):
+        return self.deterministic
+
+    def set_stream(self, stream):
+        self.stream = stream
+        call("b200_ctx_set_stream", self._ctx, _vp(stream.cuda_stream))
+
+    def synchronize(self):
+        call("b200_ctx_sync", self._ctx)
+
+    def launch_count(self):
+        n = ctypes.c_int64()
+        call("b200_ctx_launch_count", self._ctx, ctypes.byref(n))
+        return n.value
+
+    def gauss_quadrature(self, q):
+        return basis1d.gauss_quadrature(q)
+
+    def lobatto_quadrature(self, q):
+        return basis1d.lobatto_quadrature(q)
+
+    def Vector(self, size, dtype=torch.float64):
+        return Vector(self, size, dtype)
+
+    def ElemRestriction(self, nelem, elemsize, ncomp, compstride, lsize, offsets, memtype=MEM_HOST, cmode=COPY_VALUES):
+        return ElemRestriction(self, nelem, elemsize, ncomp, compstride, lsize, offsets)
+
+    def StridedElemRestriction(self, nelem, elemsize, ncomp, lsize, strides):
+        return StridedElemRestriction(self, nelem, elemsize, ncomp, lsize, strides)
+
+    def BasisTensorH1(self, dim, ncomp, P1d, Q1d, interp1d, grad1d, qref1d, qweight1d):
+        return BasisTensorH1(self, dim, ncomp, P1d, Q1d, interp1d, grad1d, qref1d, qweight1d)
+
+    def BasisTensorH1Lagrange(self, dim, ncomp, P, Q, qmode=GAUSS):
+        interp, grad, qref, qw = basis1d.lagrange_1d(P, Q, qmode)
+        return BasisTensorH1(self, dim, ncomp, P, Q, interp, grad, qref, qw)
+
+    def QFunctionByName(self, name):
+        return QFunctionByName(self, name)
+
+    def Operator(self, qf, dqf=None, qdfT=None):
+        return Operator(self, qf)
+
+    def __del__(self):
+        try:
+            if getattr(self, "_ctx", None):
+                load().b200_ctx_destroy(self._ctx)
+                self._ctx = None
+        except Exception:
+            pass
+
+
+def _prec(dtype):
+    if dtype == torch.float64:
+        return F64
+    if dtype == torch.float32:
+        return F32
+    raise B200Error("Vector", 4, f"unsupported scalar type {dtype}")
+
+
+class Vector:
+    """CeedVector with its array in device memory (a torch tensor); host access copies."""
+
+    def __init__(self, ceed, size, dtype=torch.float64):
+        self.ceed = ceed
+        self.size = int(size)
+        self.dtype = dtype
+        self.prec = _prec(dtype)
+        self.data = torch.empty(self.size, dtype=dtype, device=ceed.device)
+
+    def __len__(self):
+        return self.size
+
+    def get_length(self):
+        return self.size
+
+    def ptr(self):
+        return _vp(self.data.data_ptr())
+
+    def set_array(self, array, memtype=MEM_HOST, cmode=COPY_VALUES):
+        """Copy (or, for a device tensor with USE_POINTER, borrow) the values."""
+        if isinstance(array, torch.Tensor):
+            if cmode == USE_POINTER and array.is_cuda and array.dtype == self.dtype and array.numel() == self.size and array.is_contiguous():
+                self.data = array
+                return
+            self.data.copy_(array.reshape(-1).to(self.dtype))
+        else:
+            a = np.ascontiguousarray(np.asarray(array).reshape(-1))
+            if a.size != self.size:
+                raise B200Error("CeedVectorSetArray", 2, f"array of {a.size} entries for a vector of {self.size}")
+            self.data.copy_(torch.from_numpy(a).to(self.dtype))
+
+    def get_array_read(self, memtype=MEM_HOST):
+        if memtype == MEM_DEVICE:
+            return self.data
+        return self.data.cpu().numpy()
+
+    def get_array(self, memtype=MEM_HOST):
+        return self.get_array_read(memtype)
+
+    def set_value(self, value):
+        call("b200_vec_set_value", self.ceed._ctx, self.prec, self.size, self.ptr(), float(value))
+
+    def norm(self, normtype=NORM_2):
+        out = ctypes.c_double()
+        call("b200_vec_norm", self.ceed._ctx, self.prec, self.size, self.ptr(), normtype, ctypes.byref(out))
+        return out.value
+
+    def dot(self, other):
+        out = ctypes.c_double()
+        call("b200_vec_dot", self.ceed._ctx, self.prec, self.size, self.ptr(), other.ptr(), ctypes.byref(out))
+        return out.value
+
+    def scale(self, alpha):
+        call("b200_vec_scale", self.ceed._ctx, self.prec, self.size, self.ptr(), float(alpha))
+
+    def axpy(self, alpha, x):
+        call("b200_vec_axpy", self.ceed._ctx, self.prec, self.size, float(alpha), x.ptr(), self.ptr())
+
+    def axpby(self, alpha, beta, x):
+        call("b200_vec_axpby", self.ceed._ctx, self.prec, self.size, float(alpha), float(beta), x.ptr(), self.ptr())
+
+    def pointwise_mult(self, x, y):
+        call("b200_vec_pointwise_mult", self.ceed._ctx, self.prec, self.size, self.ptr(), x.ptr(), y.ptr())
+
+    def reciprocal(self):
+        call("b200_vec_reciprocal", self.ceed._ctx, self.prec, self.size, self.ptr())
+
+    def copy_from(self, other):
+        self.data.copy_(other.data.to(self.dtype))
+
+
+class ElemRestriction:
+    """Offset element restriction (CeedElemRestrictionCreate); E-vector layout [comp][elem][node]."""
+
+    def __init__(self, ceed, nelem, elemsize, ncomp, compstride, lsize, offsets):
+        self.ceed = ceed
+        self.nelem, self.elemsize, self.ncomp, self.compstride, self.lsize = int(nelem), int(elemsize), int(ncomp), int(compstride), int(lsize)
+        off = offsets if isinstance(offsets, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(offsets, dtype=np.int32)))
+        if off.numel() != self.nelem * self.elemsize:
+            raise B200Error("CeedElemRestrictionCreate", 2, f"{off.numel()} offsets for {self.nelem} elements of size {self.elemsize}")
+        host = off.cpu().numpy()
+        if host.size and (host.min() < 0 or int(host.max()) + (self.ncomp - 1) * self.compstride >= self.lsize):
+            raise B200Error("CeedElemRestrictionCreate", 2, "offsets fall outside the L-vector")
+        self.offsets_host = host
+        self.offsets = off.to(device=ceed.device, dtype=torch.int32).contiguous()
+        self._plan = None
+
+    def get_e_layout(self):
+        return (1, self.nelem * self.elemsize, self.elemsize)
+
+    def create_vector(self, dtype=torch.float64):
+        return Vector(self.ceed, self.lsize, dtype), Vector(self.ceed, self.nelem * self.elemsize * self.ncomp, dtype)
+
+    def plan(self):
+        if self._plan is None:
+            h = ctypes.c_void_p()
+            call("b200_plan_create", self.ceed._ctx, self.nelem, self.elemsize, self.ncomp, self.compstride, self.lsize,
+                 self.offsets_host.ctypes.data_as(ctypes.c_void_p), _vp(self.offsets.data_ptr()), ctypes.byref(h))
+            self._plan = h
+        return self._plan
+
+    def apply(self, u, v, tmode=NOTRANSPOSE, request=REQUEST_IMMEDIATE):
+        """NOTRANSPOSE: v = E u.  TRANSPOSE: v += E^T u (atomic, or the deterministic plan when the Ceed asks)."""
+        ctx = self.ceed._ctx
+        if tmode == NOTRANSPOSE:
+            call("b200_rstr_gather", ctx, u.prec, self.nelem, self.elemsize, self.ncomp, self.compstride, self.lsize,
+                 _vp(self.offsets.data_ptr()), u.ptr(), v.ptr())
+        elif self.ceed.deterministic:
+            call("b200_rstr_scatter_det", ctx, self.plan(), u.prec, u.ptr(), v.ptr(), 1)
+        else:
+            call("b200_rstr_scatter_atomic", ctx, u.prec, self.nelem, self.elemsize, self.ncomp, self.compstride, self.lsize,
+                 _vp(self.offsets.data_ptr()), u.ptr(), v.ptr())
+
+    def __del__(self):
+        try:
+            if self._plan is not None:
+                load().b200_plan_destroy(self._plan)
+        except Exception:
+            pass
+
+
+class StridedElemRestriction:
+    """Strided restriction (CeedElemRestrictionCreateStrided).  STRIDES_BACKEND is the identity on the backend
+    layout [comp][elem][node]."""
+
+    def __init__(self, ceed, nelem, elemsize, ncomp, lsize, strides):
+        self.ceed = ceed
+        self.nelem, self.elemsize, self.ncomp, self.lsize = int(nelem), int(elemsize), int(ncomp), int(lsize)
+        self.backend_strides = isinstance(strides, str) and strides == STRIDES_BACKEND
+        self.strides = (1, self.nelem * self.elemsize, self.elemsize) if self.backend_strides else tuple(int(s) for s in strides)
+        self.offsets = None
+
+    def get_e_layout(self):
+        return (1, self.nelem * self.elemsize, self.elemsize)
+
+    def apply(self, u, v, tmode=NOTRANSPOSE, request=REQUEST_IMMEDIATE):
+        s = (ctypes.c_int64 * 3)(*self.strides)
+        # (node, comp, elem) strides as the reference: index = node*s0 + comp*s1 + elem*s2
+        node_s, comp_s, elem_s = self.strides
+        arr = (ctypes.c_int64 * 3)(node_s, comp_s, elem_s)
+        name = "b200_rstr_strided_gather" if tmode == NOTRANSPOSE else "b200_rstr_strided_scatter"
+        call(name, self.ceed._ctx, u.prec, self.nelem, self.elemsize, self.ncomp, arr, u.ptr(), v.ptr())
+        del s
+
+
+class BasisTensorH1:
+    """Tensor-product H1 basis (CeedBasisCreateTensorH1); tables are row-major Q x P."""
+
+    def __init__(self, ceed, dim, ncomp, P1d, Q1d, interp1d, grad1d, qref1d, qweight1d):
+        self.ceed = ceed
+        self.dim, self.ncomp, self.P1d, self.Q1d = int(dim), int(ncomp), int(P1d), int(Q1d)
+        self.interp1d = np.ascontiguousarray(np.asarray(interp1d, dtype=np.float64).reshape(Q1d, P1d))
+        self.grad1d = np.ascontiguousarray(np.asarray(grad1d, dtype=np.float64).reshape(Q1d, P1d))
+        self.qref1d = np.ascontiguousarray(np.asarray(qref1d, dtype=np.float64))
+        self.qweight1d = np.ascontiguousarray(np.asarray(qweight1d, dtype=np.float64))
+        h = ctypes.c_void_p()
+        call("b200_basis_create", ceed._ctx, self.dim, self.P1d, self.Q1d, self.ncomp, self.interp1d.ctypes.data_as(ctypes.c_void_p),
+             self.grad1d.ctypes.data_as(ctypes.c_void_p), self.qweight1d.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
+        self._h = h
+
+    def get_num_nodes(self):
+        return self.P1d ** self.dim
+
+    def get_num_quadrature_points(self):
+        return self.Q1d ** self.dim
+
+    def get_interp_1d(self):
+        return self.interp1d
+
+    def get_grad_1d(self):
+        return self.grad1d
+
+    def get_q_ref_1d(self):
+        return self.qref1d
+
+    def get_q_weight_1d(self):
+        return self.qweight1d
+
+    def apply(self, nelem, emode, u, v, tmode=NOTRANSPOSE):
+        up = u.ptr() if u is not None else _vp(0)
+        prec = v.prec
+        call("b200_basis_apply", self._h, prec, int(nelem), tmode, emode, 0, up, v.ptr())
+
+    def apply_add(self, nelem, emode, u, v, tmode=TRANSPOSE):
+        call("b200_basis_apply", self._h, v.prec, int(nelem), tmode, emode, 1, u.ptr(), v.ptr())
+
+    def __del__(self):
+        try:
+            load().b200_basis_destroy(self._h)
+        except Exception:
+            pass
+
+
+class QFunctionByName:
+    """A gallery QFunction (CeedQFunctionCreateInteriorByName)."""
+
+    def __init__(self, ceed, name):
+        if name not in GALLERY:
+            raise B200Error("CeedQFunctionCreateInteriorByName", -2, f"no gallery QFunction named {name!r} on /gpu/cuda/b200")
+        self.ceed, self.name = ceed, name
+        self.kind, self.inputs, self.outputs = GALLERY[name]
+
+    def apply(self, q, inputs, outputs):
+        """CeedQFunctionApply on Q-vectors (field component k of point i at k*q + i)."""
+        if isinstance(self.kind, str):
+            raise B200Error("CeedQFunctionApply", -2, f"{self.name} is applied through its setup operator on this backend")
+        ins = (ctypes.c_void_p * 3)(*([x.data.data_ptr() for x in inputs] + [0] * (3 - len(inputs))))
+        outs = (ctypes.c_void_p * 1)(outputs[0].data.data_ptr())
+        call("b200_qf_apply", self.ceed._ctx, outputs[0].prec, self.kind, int(q), ins, outs)
+
+
+ACTIVE = "active"
+NONE = None
+
+
+class _Field:
+    def __init__(self, name, rstr, basis, vec):
+        self.name, self.rstr, self.basis, self.vec = name, rstr, basis, vec
+
+
+class Operator:
+    """CeedOperator on tensor-H1 hexahedra.  Apply-type gallery QFunctions run in one fused kernel per apply;
+    the gallery build QFunctions run the geometric-factor kernel.  Anything else raises (no CPU fallback)."""
+
+    def __init__(self, ceed, qf):
+        self.ceed, self.qf = ceed, qf
+        self.fields = {}
+        self._fused = {}
+        self.elems_per_block = 0
+        self.staging = 0
+
+    def set_field(self, name, rstr, basis, vec):
+        names = [f[0] for f in self.qf.inputs + self.qf.outputs]
+        if name not in names:
+            raise B200Error("CeedOperatorSetField", 2, f"QFunction {self.qf.name} has no field {name!r}")
+        self.fields[name] = _Field(name, rstr, basis, vec)
+
+    # ---- the fused path ---------------------------------------------------------------------------------------------
+    def _active_input(self):
+        return self.fields[self.qf.inputs[0][0]]
+
+    def _fused_op(self, prec):
+        key = (prec, self.ceed.deterministic, self.elems_per_block, self.staging)
+        if key in self._fused:
+            return self._fused[key]
+        f = self._active_input()
+        rstr, basis = f.rstr, f.basis
+        if not isinstance(rstr, ElemRestriction) or not isinstance(basis, BasisTensorH1) or basis.dim != 3:
+            raise B200Error("CeedOperatorApply", -2, "fused apply needs an offset restriction and a 3D tensor H1 basis")
+        d = OpDesc()
+        d.qf, d.prec, d.P_1d, d.Q_1d, d.num_comp = self.qf.kind, prec, basis.P1d, basis.Q1d, rstr.ncomp
+        d.scatter = SCATTER_DETERMINISTIC if self.ceed.deterministic else SCATTER_ATOMIC
+        d.num_elem, d.l_size, d.comp_stride = rstr.nelem, rstr.lsize, rstr.compstride
+        d.offsets = rstr.offsets.data_ptr()
+        d.interp_1d = basis.interp1d.ctypes.data
+        d.grad_1d = basis.grad1d.ctypes.data
+        d.elems_per_block, d.staging = self.elems_per_block, self.staging
+        h = ctypes.c_void_p()
+        call("b200_op_create", self.ceed._ctx, ctypes.byref(d), ctypes.byref(h))
+        op = _FusedOp(self.ceed, h, (basis.interp1d, basis.grad1d))
+        self._fused[key] = op
+        return op
+
+    def fused(self, prec=F64):
+        """The fused kernel object behind this operator (tile control, cost model)."""
+        return self._fused_op(prec)
+
+    def _passive(self, name, prec):
+        v = self.fields[name].vec
+        if v is None or isinstance(v, str):
+            raise B200Error("CeedOperatorApply", 3, f"passive field {name!r} needs a vector")
+        if v.prec != prec:
+            raise B200Error("CeedOperatorApply", 4, f"field {name!r} precision differs from the active vectors")
+        return v
+
+    def _apply(self, u, v, add):
+        kind = self.qf.kind
+        if isinstance(kind, str):
+            return self._build(u, v, add)
+        op = self._fused_op(u.prec)
+        qd = self._passive("qdata", u.prec)
+        kap = self._passive("kappa", u.prec) if kind == QF_POISSON_KAPPA else None
+        call("b200_op_apply", op.h, u.ptr(), v.ptr(), qd.ptr(), kap.ptr() if kap else _vp(0), 1 if add else 0)
+
+    def _build(self, u, v, add):
+        dx = self.fields["dx"]
+        if add:
+            raise B200Error("CeedOperatorApplyAdd", -2, "the geometric-factor setup is applied with CeedOperatorApply")
+        rx, bx = dx.rstr, dx.basis
+        if not isinstance(rx, ElemRestriction) or rx.elemsize != 8 or rx.ncomp != 3 or bx.P1d != 2 or bx.dim != 3:
+            raise B200Error("CeedOperatorApply", -2, "geometric factors need a trilinear coordinate field (P=2, 3 components)")
+        out = self.fields["qdata"].rstr
+        if not (isinstance(out, StridedElemRestriction) and out.backend_strides):
+            raise B200Error("CeedOperatorApply", -2, "qdata must use CEED_STRIDES_BACKEND on this backend")
+        if u.prec != F64 or v.prec != F64:
+            raise B200Error("CeedOperatorApply", -2, "geometric factors are computed in FP64")
+        call("b200_qdata_build", self.ceed._ctx, 1 if self.qf.kind == "build_poisson" else 0, rx.nelem, bx.Q1d,
+             bx.interp1d.ctypes.data_as(ctypes.c_void_p), bx.grad1d.ctypes.data_as(ctypes.c_void_p),
+             bx.qweight1d.ctypes.data_as(ctypes.c_void_p), _vp(rx.offsets.data_ptr()), rx.compstride, u.ptr(), v.ptr())
+
+    def apply(self, u, v, request=REQUEST_IMMEDIATE):
+        """CeedOperatorApply: v = A u."""
+        self._apply(u, v, False)
+
+    def apply_add(self, u, v, request=REQUEST_IMMEDIATE):
+        """CeedOperatorApplyAdd: v += A u."""
+        self._apply(u, v, True)
+
+    def kappa_grad(self, u, w, g):
+        """g[elem][qpt] = grad(w) . D grad(u): the kappa-adjoint of the kappa-weighted diffusion."""
+        op = self._fused_op(u.prec)
+        qd = self._passive("qdata", u.prec)
+        call("b200_op_kappa_grad", op.h, u.ptr(), w.ptr(), qd.ptr(), g.ptr())
+
+
+class _FusedOp:
+    def __init__(self, ceed, h, keep):
+        self.ceed, self.h, self._keep = ceed, h, keep
+
+    def cost(self):
+        b, f = ctypes.c_double(), ctypes.c_double()
+        call("b200_op_cost", self.h, ctypes.byref(b), ctypes.byref(f))
+        return b.value, f.value
+
+    def tile(self):
+        e, t, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        call("b200_op_get_tile", self.h, ctypes.byref(e), ctypes.byref(t), ctypes.byref(s))
+        return e.value, t.value, s.value
+
+    def set_tile(self, elems_per_block, staging=0):
+        call("b200_op_set_tile", self.h, int(elems_per_block), int(staging))
+
+    def __del__(self):
+        try:
+            load().b200_op_destroy(self.h)
+        except Exception:
+            pass

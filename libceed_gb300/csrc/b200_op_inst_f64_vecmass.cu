@@ -1,0 +1,4 @@
+// Compiled instances of the fused operator kernel: double, B200_QF_VECMASS, P_1d = 2..9, register and shared-memory qdata staging.
+#include "b200_op_launch.cuh"
+
+B200_OP_TABLE(double, B200_QF_VECMASS, op_table_f64_vecmass)

@@ -1,0 +1,254 @@
+// Fused operator apply: object lifetime, launch-shape selection and the deterministic scatter.
+//
+// Takes over CeedOperatorApplyAdd_Cuda_gen / ApplyAddCore (backends/cuda-gen/ceed-cuda-gen-operator.c:105-300):
+// one fused kernel launch per apply, block shape chosen per (precision, P, Q, components) instead of the reference's
+// occupancy-and-waste heuristic (:40-97).  With the deterministic scatter the fused kernel writes the element results
+// and the inverse-offset plan sums them in a fixed order.
+#include "b200_internal.cuh"
+#include "b200_op_launch.cuh"
+#include "b200_plan.cuh"
+
+#include <cmath>
+#include <vector>
+
+namespace b200 {
+bool op_table_f64_mass(int, int, OpInstance *);
+bool op_table_f64_poisson(int, int, OpInstance *);
+bool op_table_f64_vecmass(int, int, OpInstance *);
+bool op_table_f64_vecpoisson(int, int, OpInstance *);
+bool op_table_f64_kappa(int, int, OpInstance *);
+bool op_table_f32_mass(int, int, OpInstance *);
+bool op_table_f32_poisson(int, int, OpInstance *);
+bool op_table_f32_vecmass(int, int, OpInstance *);
+bool op_table_f32_vecpoisson(int, int, OpInstance *);
+bool op_table_f32_kappa(int, int, OpInstance *);
+bool kgrad_table_f64(int, OpLauncher *);
+bool kgrad_table_f32(int, OpLauncher *);
+
+bool op_lookup(int prec, int qf, int P, int stage, OpInstance *out) {
+  if (P < kOpPMin || P > kOpPMax) return false;
+  if (prec == B200_F64) {
+    switch (qf) {
+      case B200_QF_MASS: return op_table_f64_mass(P, stage, out);
+      case B200_QF_POISSON: return op_table_f64_poisson(P, stage, out);
+      case B200_QF_VECMASS: return op_table_f64_vecmass(P, stage, out);
+      case B200_QF_VECPOISSON: return op_table_f64_vecpoisson(P, stage, out);
+      case B200_QF_POISSON_KAPPA: return op_table_f64_kappa(P, stage, out);
+    }
+  } else if (prec == B200_F32) {
+    switch (qf) {
+      case B200_QF_MASS: return op_table_f32_mass(P, stage, out);
+      case B200_QF_POISSON: return op_table_f32_poisson(P, stage, out);
+      case B200_QF_VECMASS: return op_table_f32_vecmass(P, stage, out);
+      case B200_QF_VECPOISSON: return op_table_f32_vecpoisson(P, stage, out);
+      case B200_QF_POISSON_KAPPA: return op_table_f32_kappa(P, stage, out);
+    }
+  }
+  return false;
+}
+
+bool kgrad_lookup(int prec, int P, OpLauncher *out) {
+  if (P < kOpPMin || P > kOpPMax) return false;
+  return prec == B200_F64 ? kgrad_table_f64(P, out) : prec == B200_F32 ? kgrad_table_f32(P, out) : false;
+}
+
+// Collocated derivative G_c = G B^+ (Q x Q), B^+ = (B^T B)^{-1} B^T by Gauss-Jordan with partial pivoting.  Same
+// matrix as CeedBasisGetCollocatedGrad (interface/ceed-basis.c:750-772), up to rounding.
+static bool collocated_grad(int P, int Q, const double *B, const double *G, double *Gc) {
+  std::vector<double> N((size_t)P * 2 * P, 0.0), pinv((size_t)P * Q, 0.0);
+  for (int i = 0; i < P; i++) {
+    for (int j = 0; j < P; j++) {
+      double s = 0.0;
+      for (int q = 0; q < Q; q++) s += B[q * P + i] * B[q * P + j];
+      N[i * 2 * P + j] = s;
+    }
+    N[i * 2 * P + P + i] = 1.0;
+  }
+  for (int c = 0; c < P; c++) {
+    int piv = c;
+    for (int r = c + 1; r < P; r++)
+      if (fabs(N[r * 2 * P + c]) > fabs(N[piv * 2 * P + c])) piv = r;
+    if (fabs(N[piv * 2 * P + c]) < 1e-300) return false;
+    if (piv != c)
+      for (int k = 0; k < 2 * P; k++) std::swap(N[c * 2 * P + k], N[piv * 2 * P + k]);
+    const double d = N[c * 2 * P + c];
+    for (int k = 0; k < 2 * P; k++) N[c * 2 * P + k] /= d;
+    for (int r = 0; r < P; r++) {
+      if (r == c) continue;
+      const double f = N[r * 2 * P + c];
+      for (int k = 0; k < 2 * P; k++) N[r * 2 * P + k] -= f * N[c * 2 * P + k];
+    }
+  }
+  for (int i = 0; i < P; i++)
+    for (int q = 0; q < Q; q++) {
+      double s = 0.0;
+      for (int k = 0; k < P; k++) s += N[i * 2 * P + P + k] * B[q * P + k];
+      pinv[i * Q + q] = s;
+    }
+  for (int i = 0; i < Q; i++)
+    for (int j = 0; j < Q; j++) {
+      double s = 0.0;
+      for (int k = 0; k < P; k++) s += G[i * P + k] * pinv[k * Q + j];
+      Gc[i * Q + j] = s;
+    }
+  return true;
+}
+
+}  // namespace b200
+
+using namespace b200;
+
+struct b200_op_s {
+  b200_ctx            ctx;
+  b200_op_desc        d;
+  std::vector<double> B, Gc;  // host copies: Q x P interp, Q x Q collocated gradient
+  OpInstance          inst;
+  int                 stage, epb;
+  b200_plan           plan;     // deterministic scatter only
+  void               *e_work;   // element results for the deterministic scatter, [comp][elem][node]
+};
+
+static int op_select(b200_op op, int epb, int stage) {
+  const int Q = op->d.Q_1d, Q2 = Q * Q;
+  if (stage != kStageReg && stage != kStageSmem) stage = op->d.num_comp > 1 ? kStageSmem : kStageReg;
+  OpInstance inst;
+  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, stage, &inst), B200_ERROR_UNSUPPORTED,
+             "no compiled fused kernel for prec=%d qf=%d P=%d Q=%d", op->d.prec, op->d.qf, op->d.P_1d, op->d.Q_1d);
+  const int max_epb_threads = inst.max_threads / Q2;
+  int       max_epb_smem    = 1;
+  while (max_epb_smem < 64 && inst.smem(max_epb_smem + 1) <= 160 * 1024) max_epb_smem++;
+  if (epb <= 0) epb = 256 / Q2 > 0 ? 256 / Q2 : 1;
+  if (epb > max_epb_threads) epb = max_epb_threads;
+  if (epb > max_epb_smem) epb = max_epb_smem;
+  B200_CHECK(epb >= 1 && inst.smem(epb) <= 227 * 1024, B200_ERROR_UNSUPPORTED, "fused kernel P=%d does not fit one element per block", op->d.P_1d);
+  op->inst  = inst;
+  op->stage = stage;
+  op->epb   = epb;
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *out) {
+  const b200_op_desc &d = *desc;
+  B200_CHECK(d.prec == B200_F64 || d.prec == B200_F32, B200_ERROR_UNSUPPORTED, "unknown precision %d", d.prec);
+  B200_CHECK(d.Q_1d == d.P_1d + 1, B200_ERROR_UNSUPPORTED, "fused kernels are compiled for Q_1d = P_1d + 1 (got P=%d, Q=%d)", d.P_1d, d.Q_1d);
+  B200_CHECK(d.P_1d >= kOpPMin && d.P_1d <= kOpPMax, B200_ERROR_UNSUPPORTED, "fused kernels cover P_1d in %d..%d (got %d)", kOpPMin, kOpPMax, d.P_1d);
+  const int nc_expected = (d.qf == B200_QF_VECMASS || d.qf == B200_QF_VECPOISSON) ? 3 : 1;
+  B200_CHECK(d.num_comp == nc_expected, B200_ERROR_DIMENSION, "QFunction %d needs %d components (got %d)", d.qf, nc_expected, d.num_comp);
+  B200_CHECK(d.offsets && d.interp_1d && d.grad_1d, B200_ERROR_INCOMPLETE, "b200_op_create: offsets and 1D matrices are required");
+  B200_CHECK(d.scatter == B200_SCATTER_ATOMIC || d.scatter == B200_SCATTER_DETERMINISTIC, B200_ERROR_UNSUPPORTED, "unknown scatter mode %d",
+             d.scatter);
+  B200_CHECK(d.num_elem >= 0 && d.num_elem <= (int64_t)INT32_MAX * 64, B200_ERROR_DIMENSION, "num_elem %lld out of range", (long long)d.num_elem);
+  b200_op op = new b200_op_s();
+  op->ctx    = ctx;
+  op->d      = d;
+  op->plan   = nullptr;
+  op->e_work = nullptr;
+  const int P = d.P_1d, Q = d.Q_1d;
+  op->B.assign(d.interp_1d, d.interp_1d + Q * P);
+  op->Gc.assign((size_t)Q * Q, 0.0);
+  if (!collocated_grad(P, Q, d.interp_1d, d.grad_1d, op->Gc.data())) {
+    delete op;
+    set_error("collocated gradient: interpolation matrix is rank deficient");
+    return B200_ERROR_BACKEND;
+  }
+  int st = op_select(op, d.elems_per_block, d.staging);
+  if (!st && d.scatter == B200_SCATTER_DETERMINISTIC && d.num_elem > 0) {
+    st = b200_plan_create(ctx, d.num_elem, P * P * P, d.num_comp, d.comp_stride, d.l_size, nullptr, d.offsets, &op->plan);
+    const size_t esz = (d.prec == B200_F64 ? 8 : 4) * (size_t)d.num_elem * P * P * P * d.num_comp;
+    if (!st) st = cuda_status(cudaMalloc(&op->e_work, esz), "cudaMalloc(e_work)", __FILE__, __LINE__);
+  }
+  if (st) {
+    b200_op_destroy(op);
+    return st;
+  }
+  *out = op;
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_set_tile(b200_op op, int elems_per_block, int staging) { return op_select(op, elems_per_block, staging); }
+
+extern "C" int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_per_block, int *staging) {
+  if (elems_per_block) *elems_per_block = op->epb;
+  if (threads_per_block) *threads_per_block = op->epb * op->d.Q_1d * op->d.Q_1d;
+  if (staging) *staging = op->stage;
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add) {
+  b200_ctx            ctx = op->ctx;
+  const b200_op_desc &d   = op->d;
+  B200_CHECK(u && v && qdata, B200_ERROR_INCOMPLETE, "b200_op_apply: u, v and qdata are required");
+  B200_CHECK(d.qf != B200_QF_POISSON_KAPPA || kappa, B200_ERROR_INCOMPLETE, "kappa-weighted diffusion needs kappa");
+  const size_t tsz = d.prec == B200_F64 ? 8 : 4;
+  if (d.num_elem == 0) {
+    if (!add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
+    return B200_SUCCESS;
+  }
+  OpLaunch r{};
+  r.num_elem    = d.num_elem;
+  r.comp_stride = d.comp_stride;
+  r.epb         = op->epb;
+  r.det         = d.scatter == B200_SCATTER_DETERMINISTIC;
+  r.offsets     = d.offsets;
+  r.u           = u;
+  r.qdata       = qdata;
+  r.kappa       = kappa;
+  r.v           = v;
+  r.e_out       = op->e_work;
+  r.B           = op->B.data();
+  r.G           = op->Gc.data();
+  if (!r.det && !add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
+  int st = op->inst.launch(ctx, r);
+  if (st) return st;
+  if (r.det) st = plan_scatter(op->plan, d.prec, op->e_work, v, add);
+  return st;
+}
+
+extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qdata, void *g) {
+  b200_ctx            ctx = op->ctx;
+  const b200_op_desc &d   = op->d;
+  B200_CHECK(d.qf == B200_QF_POISSON_KAPPA, B200_ERROR_INCOMPATIBLE, "kappa gradient needs the kappa-weighted diffusion operator");
+  if (d.num_elem == 0) return B200_SUCCESS;
+  OpLauncher launch;
+  B200_CHECK(kgrad_lookup(d.prec, d.P_1d, &launch), B200_ERROR_UNSUPPORTED, "no kappa-gradient kernel for P=%d", d.P_1d);
+  OpLaunch r{};
+  r.num_elem    = d.num_elem;
+  r.comp_stride = d.comp_stride;
+  const int Q   = d.Q_1d;
+  r.epb         = 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1;
+  while (r.epb > 1 && (size_t)(d.prec == B200_F64 ? 8 : 4) * r.epb * 3 * Q * Q * Q > 96 * 1024) r.epb--;
+  r.offsets = d.offsets;
+  r.u       = u;
+  r.w       = w;
+  r.qdata   = qdata;
+  r.g       = g;
+  r.B       = op->B.data();
+  r.G       = op->Gc.data();
+  return launch(ctx, r);
+}
+
+extern "C" int b200_op_cost(b200_op op, double *bytes, double *flops) {
+  const b200_op_desc &d  = op->d;
+  const double        P  = d.P_1d, Q = d.Q_1d, ne = (double)d.num_elem, nc = d.num_comp;
+  const double        ts = d.prec == B200_F64 ? 8.0 : 4.0;
+  const bool          grad = d.qf == B200_QF_POISSON || d.qf == B200_QF_VECPOISSON || d.qf == B200_QF_POISSON_KAPPA;
+  const double        nqd  = grad ? 6.0 : 1.0;
+  // Algorithmic bytes: read u, write v, read offsets, read qdata (and kappa) once each.
+  if (bytes) *bytes = ts * (2.0 * (double)d.l_size) + 4.0 * ne * P * P * P + ts * ne * Q * Q * Q * (nqd + (d.qf == B200_QF_POISSON_KAPPA ? 1 : 0));
+  if (flops) {
+    const double interp = 2.0 * (P * P * P * Q + P * P * Q * Q + P * Q * Q * Q);  // one direction set, one way
+    const double gradc  = 3.0 * 2.0 * Q * Q * Q * Q;                              // collocated derivatives, one way
+    const double qf     = grad ? (15.0 + (d.qf == B200_QF_POISSON_KAPPA ? 6.0 : 0.0)) * Q * Q * Q : 1.0 * Q * Q * Q;
+    const double per_c  = 2.0 * interp + (grad ? 2.0 * gradc + 2.0 * Q * Q * Q : 0.0);
+    *flops              = ne * (nc * per_c + (grad ? nc * 15.0 * Q * Q * Q : nc * Q * Q * Q) + (qf - (grad ? 15.0 : 1.0) * Q * Q * Q));
+  }
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_destroy(b200_op op) {
+  if (!op) return B200_SUCCESS;
+  if (op->plan) b200_plan_destroy(op->plan);
+  if (op->e_work) cudaFree(op->e_work);
+  delete op;
+  return B200_SUCCESS;
+}

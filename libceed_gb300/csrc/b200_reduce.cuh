@@ -1,0 +1,61 @@
+// Deterministic two-pass reductions (sum of squares, |x| sum, max |x|, dot product), accumulated in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "b200_internal.cuh"
+
+namespace b200 {
+
+enum { kRedSumSq = 0, kRedAbsSum = 1, kRedMaxAbs = 2, kRedDot = 3 };
+constexpr int kReduceThreads = 256;
+
+// Fixed grid: two blocks per SM.  The result of a reduction depends only on n and the grid, never on timing.
+inline int reduce_blocks(int num_sms) { return 2 * num_sms; }
+
+__device__ __forceinline__ double red_combine(int kind, double a, double b) { return kind == kRedMaxAbs ? fmax(a, b) : a + b; }
+
+// Block-wide combine in a fixed tree: warp shuffles, then the warp leaders.
+__device__ __forceinline__ double block_reduce(int kind, double v) {
+  __shared__ double s_warp[kReduceThreads / 32];
+  for (int off = 16; off > 0; off >>= 1) v = red_combine(kind, v, __shfl_down_sync(0xffffffffu, v, off));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) s_warp[warp] = v;
+  __syncthreads();
+  v = threadIdx.x < kReduceThreads / 32 ? s_warp[threadIdx.x] : 0.0;
+  if (warp == 0)
+    for (int off = 16; off > 0; off >>= 1) v = red_combine(kind, v, __shfl_down_sync(0xffffffffu, v, off));
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_partial(int kind, int64_t n, const T *__restrict__ x, const T *__restrict__ y,
+                                                                   double *__restrict__ partial) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double xi = (double)x[i];
+    switch (kind) {
+      case kRedSumSq: acc += xi * xi; break;
+      case kRedAbsSum: acc += fabs(xi); break;
+      case kRedMaxAbs: acc = fmax(acc, fabs(xi)); break;
+      default: acc += xi * (double)y[i]; break;
+    }
+  }
+  acc = block_reduce(kind, acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_final(int kind, int blocks, const double *__restrict__ partial,
+                                                                 double *__restrict__ result) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < blocks; i += blockDim.x) acc = red_combine(kind, acc, partial[i]);
+  acc = block_reduce(kind, acc);
+  if (threadIdx.x == 0) result[0] = acc;
+}
+
+// Reduce into result_dev (device memory) on the context stream, without a host round trip.
+int reduce_to_device(b200_ctx ctx, int prec, int kind, int64_t n, const void *x, const void *y, double *result_dev);
+
+}  // namespace b200

@@ -1,0 +1,63 @@
+"""The C ABI library loads on a host without a GPU and exports every entry point include/ceed-b200.h declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from libceed_gb300 import _ffi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", h)).read(), flags=re.S)
+            names |= set(re.findall(r"^\s*(?:int|const char \*)\s*(b200_\w+)\s*\(", text, flags=re.M))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_ffi.LIB_PATH):
+        from libceed_gb300 import build
+
+        build.build()
+    return _ffi.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 30
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_parser_sees_every_declaration():
+    assert {d[0] for d in _ffi.declarations()} == _declared()
+
+
+def test_calls_fail_loudly_without_a_device(lib):
+    """With no GPU the context cannot be created; the call reports an error instead of falling back."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    with pytest.raises(_ffi.B200Error):
+        _ffi.call("b200_ctx_create", 0, ctypes.byref(h))
+
+
+def test_ceed_refuses_without_gpu():
+    import torch
+
+    import libceed_gb300 as ceed
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(ceed.B200Error):
+        ceed.Ceed("/gpu/cuda/b200")
+    with pytest.raises(ceed.B200Error):
+        ceed.Ceed("/cpu/self/ref/serial")

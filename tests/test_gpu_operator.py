@@ -1,0 +1,136 @@
+"""Fused operator apply on the GPU against the reference's golden vectors and the oracle.
+
+Tolerances: FP64 applies within 1e-12 relative l-infinity of the reference (`/cpu/self/ref/serial`);
+FP32 applies within 5e-5; gathers and the deterministic scatter into a zero vector are bit-exact.
+"""
+import numpy as np
+import pytest
+import torch
+
+import libceed_gb300 as lc
+from tests.conftest import relinf
+from tests.gpu_cases import CASES, ref_layout_to_backend, setup
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ceed():
+    return lc.Ceed("/gpu/cuda/b200")
+
+
+@pytest.fixture(scope="module")
+def ceed_det():
+    return lc.Ceed("/gpu/cuda/b200", deterministic=True)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_qdata_setup_matches_reference(ceed, case):
+    kind, box, g, objs = setup(ceed, case)
+    nqd = 6 if kind in ("poisson", "vpoisson", "kappa") else 1
+    want = ref_layout_to_backend(g["qdata"], box.num_elem, nqd, box.Q ** 3)
+    assert relinf(objs["qdata"].get_array_read(), want) < 1e-13
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("det", [False, True])
+def test_fp64_apply_matches_reference(ceed, ceed_det, case, det):
+    c = ceed_det if det else ceed
+    kind, box, g, objs = setup(c, case)
+    u = c.Vector(box.l_size)
+    u.set_array(box.u())
+    v = c.Vector(box.l_size)
+    v.set_value(123.0)  # Apply must overwrite
+    objs["op"].apply(u, v)
+    assert relinf(v.get_array_read(), g["v"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["poisson_n3_p4", "vpoisson_n4_p2", "mass_n8_p3", "kappa_n3_p3"])
+def test_fp32_apply_matches_reference(ceed, case):
+    kind, box, g, objs = setup(ceed, case, dtype=torch.float32)
+    u = ceed.Vector(box.l_size, torch.float32)
+    u.set_array(box.u())
+    v = ceed.Vector(box.l_size, torch.float32)
+    objs["op"].apply(u, v)
+    assert relinf(v.get_array_read(), g["v"]) < 5e-5
+
+
+@pytest.mark.parametrize("case", ["poisson_n3_p4", "vpoisson_n3_p4"])
+def test_deterministic_apply_is_bit_reproducible(ceed_det, case):
+    kind, box, g, objs = setup(ceed_det, case)
+    u = ceed_det.Vector(box.l_size)
+    u.set_array(box.u())
+    outs = []
+    for _ in range(3):
+        v = ceed_det.Vector(box.l_size)
+        objs["op"].apply(u, v)
+        outs.append(v.get_array_read())
+    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+
+
+@pytest.mark.parametrize("det", [False, True])
+def test_apply_add_accumulates(ceed, ceed_det, det):
+    c = ceed_det if det else ceed
+    kind, box, g, objs = setup(c, "poisson_n3_p3")
+    u = c.Vector(box.l_size)
+    u.set_array(box.u())
+    v = c.Vector(box.l_size)
+    v0 = lc.mesh.uniform(77, box.l_size)
+    v.set_array(v0)
+    objs["op"].apply_add(u, v)
+    assert relinf(v.get_array_read(), v0 + g["v"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["mass_n8_p3", "vpoisson_n4_p2", "poisson_n3_p4"])
+def test_restriction_gather_and_scatter_bit_exact(ceed, ceed_det, case):
+    for c in (ceed, ceed_det):
+        kind, box, g, objs = setup(c, case)
+        ru = objs["ru"]
+        u = c.Vector(box.l_size)
+        u.set_array(box.u())
+        e = c.Vector(box.num_elem * box.P ** 3 * box.ncomp)
+        ru.apply(u, e, lc.NOTRANSPOSE)
+        want_e = ref_layout_to_backend(g["egather"], box.num_elem, box.ncomp, box.P ** 3)
+        assert np.array_equal(e.get_array_read(), want_e)
+        l = c.Vector(box.l_size)
+        l.set_value(0.0)
+        ru.apply(e, l, lc.TRANSPOSE)
+        if c.deterministic:
+            # Fixed per-node order = the reference's element order: bit-exact.
+            assert np.array_equal(l.get_array_read(), g["escatter"])
+        else:
+            assert relinf(l.get_array_read(), g["escatter"]) < 1e-15
+
+
+def test_unsupported_configurations_raise(ceed):
+    from libceed_gb300 import mesh
+
+    box = mesh.Box(2, 3)
+    ru = ceed.ElemRestriction(box.num_elem, box.P ** 3, 1, 1, box.l_size, box.offsets())
+    b = ceed.BasisTensorH1Lagrange(3, 1, box.P, box.P + 3, lc.GAUSS)  # Q = P + 3: no compiled fused kernel
+    op = ceed.Operator(ceed.QFunctionByName("MassApply"))
+    q = ceed.Vector(box.num_elem * (box.P + 3) ** 3)
+    op.set_field("u", ru, b, "active")
+    op.set_field("qdata", ceed.StridedElemRestriction(box.num_elem, (box.P + 3) ** 3, 1, q.size, lc.STRIDES_BACKEND), None, q)
+    op.set_field("v", ru, b, "active")
+    u, v = ceed.Vector(box.l_size), ceed.Vector(box.l_size)
+    with pytest.raises(lc.B200Error):
+        op.apply(u, v)
+    with pytest.raises(lc.B200Error):
+        ceed.ElemRestriction(1, 8, 1, 1, 4, np.arange(8, dtype=np.int32))  # offsets beyond the L-vector
+
+
+@pytest.mark.parametrize("det", [False, True])
+def test_kappa_gradient_matches_reference(ceed, ceed_det, det):
+    c = ceed_det if det else ceed
+    kind, box, g, objs = setup(c, "kappa_n3_p3")
+    u = c.Vector(box.l_size)
+    u.set_array(box.u())
+    y = c.Vector(box.l_size)
+    objs["op"].apply(u, y)
+    f = lc.mesh.uniform(4003 + 3, box.l_size)
+    w = c.Vector(box.l_size)
+    w.set_array(y.get_array_read() - f)
+    gk = c.Vector(box.num_elem * box.Q ** 3)
+    objs["op"].kappa_grad(u, w, gk)
+    assert relinf(gk.get_array_read(), g["kgrad"]) < 1e-12
