@@ -1,0 +1,382 @@
+"""Benchmark of the `/gpu/cuda/b200` operator-apply path: 3D Poisson apply GDoF/s (FP64) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--degree P] [--no-extras]
+
+A step is one CeedOperatorApply of the degree-`P` (default 4) diffusion operator on a structured box of
+hexahedra sized to ~17M DoF (n=64 elements per direction at degree 4: 16,974,593 DoF), geometric factors
+from the gallery Poisson3DBuild on a trilinear mesh with +-0.05h interior-vertex noise, input uniform on
+[-1, 1] (seeded synthetic data; the reference publishes no dataset for this path).  Inputs (2.7 GB of
+qdata at degree 4) are far larger than L2, so no flush is needed between steps.
+
+`value` is device time of K applies with inputs resident in HBM (CUDA events, max over ranks).  `e2e`
+times the same applies through the public API with the input copied from pinned host memory and the
+result copied back every step.  Ranks (N>1) apply independent replicas of the problem: the operator
+is element-parallel with no exchange inside an apply, so there is no collective (weak scaling).
+
+--impl reference times the reference algorithm on the host cores instead: the oracle restatement of
+libCEED's /cpu/self/ref/serial backend (the reference library itself is x86-only here and cannot be
+run on the GPU host), one process per core, each applying the operator to its own sub-box.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_FOR_DEGREE = {1: 256, 2: 128, 3: 85, 4: 64, 5: 52, 6: 43, 7: 37, 8: 32}
+METRIC = "GDoF/s per operator apply (3D Poisson p=1..8), FP32+refine vs FP64 CG time"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--degree", type=int, default=4)
+    ap.add_argument("--no-extras", action="store_true", help="skip the per-degree sweep and the CG solve comparison")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------------------------------------
+# CPU side: the reference algorithm (oracle restatement of /cpu/self/ref/serial), one process per core
+# ------------------------------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    n, degree, reps, seed = args
+    from oracle import oracle as orc
+
+    pb = orc.BoxProblem(n, degree, poisson=True, noise=0.05, seed=seed)
+    pb.apply()  # warm
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        pb.apply()
+    return pb.l_size * reps, time.perf_counter() - t0
+
+
+def cpu_reference_rate(degree, seconds_target=12.0, cores=None):
+    """Aggregate DoF/s of the oracle apply with one process per core on independent sub-boxes."""
+    import multiprocessing as mp
+
+    cores = cores or os.cpu_count() or 1
+    n = max(2, {1: 40, 2: 20, 3: 14, 4: 10, 5: 8, 6: 7, 7: 6, 8: 5}.get(degree, 8))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        # calibrate on one process
+        dof, dt = pool.map(_cpu_worker, [(n, degree, 1, 100)])[0]
+        reps = max(1, int(seconds_target / max(dt, 1e-3)))
+        res = pool.map(_cpu_worker, [(n, degree, reps, 100 + i) for i in range(cores)])
+    total = sum(r[0] for r in res)
+    tmax = max(r[1] for r in res)
+    sample = f"{cores} processes x {reps} applies of a degree-{degree} box with n={n} ({res[0][0] // reps} DoF each)"
+    return total / tmax / 1e9, cores, sample
+
+
+# ------------------------------------------------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ------------------------------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic(key):
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary (profiles/traffic.json)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------------------------------------------------------
+# GPU side
+# ------------------------------------------------------------------------------------------------------------------
+def gpu_main(a, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import libceed_gb300 as lc
+    from libceed_gb300 import mesh
+    from libceed_gb300.smoke_case import build_poisson
+
+    torch.cuda.set_device(local_rank)
+    ceed = lc.Ceed(f"/gpu/cuda/b200:device_id={local_rank}")
+    degree = a.degree
+    n = N_FOR_DEGREE[degree]
+    box = mesh.Box(n, degree, noise=0.05, seed=2000 + degree + 17 * rank)
+    objs = build_poisson(ceed, box)
+    op = objs["op"]
+    u = ceed.Vector(box.l_size)
+    u.set_array(box.u())
+    v = ceed.Vector(box.l_size)
+    fused = op.fused(lc.F64)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(a.warmup):
+        op.apply(u, v)
+    launches0 = ceed.launch_count()
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        op.apply(u, v)
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    ms_total = e0.elapsed_time(e1)
+    launches = ceed.launch_count() - launches0
+
+    # Kernel-only time of the fused kernel (apply_add: no zeroing of v), for the roofline.
+    for _ in range(2):
+        op.apply_add(u, v)
+    torch.cuda.synchronize()
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for _ in range(a.steps):
+        op.apply_add(u, v)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    kernel_ms = k0.elapsed_time(k1) / a.steps
+
+    # End to end through the public API: pinned host input -> device, apply, result -> pinned host, every step.
+    u_host = torch.from_numpy(box.u()).pin_memory()
+    v_host = torch.empty(box.l_size, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        u.data.copy_(u_host, non_blocking=True)
+        op.apply(u, v)
+        v_host.copy_(v.data, non_blocking=True)
+    barrier()
+    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x0.record(stream)
+    for _ in range(a.steps):
+        u.data.copy_(u_host, non_blocking=True)
+        op.apply(u, v)
+        v_host.copy_(v.data, non_blocking=True)
+    x1.record(stream)
+    barrier()
+    e2e_ms = x0.elapsed_time(x1)
+
+    t = torch.tensor([ms_total, e2e_ms, kernel_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_total, e2e_ms, kernel_ms = t.tolist()
+
+    extras = {}
+    if rank == 0 and not a.no_extras:
+        extras = run_extras(ceed, lc, mesh, build_poisson, torch, np)
+
+    if rank != 0:
+        return None
+    dof_total = box.l_size * world * a.steps
+    value = dof_total / (ms_total * 1e-3) / 1e9
+    bytes_alg, flops_alg = fused.cost()
+    peaks, peak_kind = measured_peaks()
+    achieved = bytes_alg / (kernel_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(f"poisson_f64_p{degree}_atomic")
+    cpu_rate, cores, sample = cpu_reference_rate(degree)
+    epb, tpb, staging = fused.tile()
+    line = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "GDoF/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": round(ms_total / a.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded box mesh, +-0.05h vertex noise, u ~ U[-1,1])",
+        "config": {"workload": f"3D Poisson apply, degree {degree} (P={degree + 1}, Q={degree + 2} Gauss), {n}^3 hexes, "
+                               f"{box.l_size} DoF, FP64, atomic scatter",
+                   "degree": degree, "elements": box.num_elem, "dof": box.l_size, "scatter": "atomic",
+                   "l2": "inputs larger than L2 (qdata %.2f GB)" % (6 * 8 * box.num_elem * box.Q ** 3 / 1e9),
+                   "parallelism": f"replicas x{world}", "tile": {"elems_per_block": epb, "threads_per_block": tpb, "staging": staging}},
+        "e2e": {"value": round(box.l_size * world * a.steps / (e2e_ms * 1e-3) / 1e9, 4), "unit": "GDoF/s",
+                "h2d_bytes_per_step": 8 * box.l_size, "d2h_bytes_per_step": 8 * box.l_size},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": round(achieved / peaks.get("hbm_gbs"), 4), "peak_kind": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes": bytes_alg, "kernel_ms": round(kernel_ms, 4),
+                     "fp64_tflops": round(flops_alg / (kernel_ms * 1e-3) / 1e12, 4)},
+        "cpu_baseline": {"value": round(cpu_rate, 5), "unit": "GDoF/s", "cores": cores, "kind": "port", "sample": sample},
+        "clocks": clocks,
+    }
+    line.update(extras)
+    return line
+
+
+def _time_applies(torch, op, u, v, reps):
+    for _ in range(3):
+        op.apply(u, v)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        op.apply(u, v)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_extras(ceed, lc, mesh, build_poisson, torch, np):
+    """Secondary measurements: per-degree apply rates (FP64 atomic / deterministic, FP32) and the FP64-vs-mixed
+    CG solve of the degree-4 problem with Dirichlet boundaries (b = A x* + noise, rtol 1e-10)."""
+    from libceed_gb300.solver import cg_solve
+
+    out = {"sweep": [], "solve": None}
+    ceed_det = lc.Ceed(ceed.resource, deterministic=True)
+    for p in range(1, 9):
+        n = N_FOR_DEGREE[p]
+        box = mesh.Box(n, p, noise=0.05, seed=2000 + p)
+        row = {"degree": p, "dof": box.l_size}
+        for tag, c, dt in (("f64_atomic", ceed, torch.float64), ("f64_det", ceed_det, torch.float64), ("f32_atomic", ceed, torch.float32)):
+            objs = build_poisson(c, box, dtype=dt)
+            u = c.Vector(box.l_size, dt)
+            u.set_array(box.u())
+            v = c.Vector(box.l_size, dt)
+            ms = _time_applies(torch, objs["op"], u, v, 10)
+            fused = objs["op"].fused(lc.F32 if dt == torch.float32 else lc.F64)
+            b, f = fused.cost()
+            row[tag] = {"gdofs": round(box.l_size / ms / 1e6, 4), "ms": round(ms, 4), "GBps_alg": round(b / ms / 1e6, 1),
+                        "tflops": round(f / ms / 1e9, 4), "tile": list(fused.tile())}
+            del objs, u, v, fused
+        out["sweep"].append(row)
+        torch.cuda.empty_cache()
+    # Mixed-precision solve (config: degree 4, 16.97M DoF, smooth manufactured solution + U[-1e-3, 1e-3] noise).
+    p, n = 4, N_FOR_DEGREE[4]
+    box = mesh.Box(n, p, noise=0.05, seed=3004)
+    o64 = build_poisson(ceed, box)
+    o32 = build_poisson(ceed, box, dtype=torch.float32)
+    m = mesh.box_mask(n, p)
+    xs = mesh.smooth_field(n, p, seed=77) * m
+    mask, xv, b = ceed.Vector(box.l_size), ceed.Vector(box.l_size), ceed.Vector(box.l_size)
+    mask.set_array(m)
+    xv.set_array(xs)
+    o64["op"].apply(xv, b)
+    b.set_array(m * (b.get_array_read() + mesh.uniform(78, box.l_size, -1e-3, 1e-3)))
+    res = {}
+    for tag, mixed in (("fp64_cg", False), ("fp32_refined_cg", True)):
+        x = ceed.Vector(box.l_size)
+        st = cg_solve(ceed, o64["op"], o64["qdata"], mask, b, x, mixed=mixed, op32=o32["op"], qdata32=o32["qdata"], rtol=1e-10,
+                      inner_rtol=1e-4, max_it=20000, use_graph=True, check_every=25)
+        res[tag] = {k: (round(v, 6) if isinstance(v, float) else v) for k, v in st.items()}
+    res["speedup_mixed_over_fp64"] = round(res["fp64_cg"]["seconds"] / res["fp32_refined_cg"]["seconds"], 3)
+    res["config"] = f"degree 4, {n}^3 hexes, {box.l_size} DoF, homogeneous Dirichlet, rtol 1e-10, graphs of 25 iterations"
+    out["solve"] = res
+    return out
+
+
+def reference_main(a, rank, world):
+    if rank != 0:
+        return None
+    cpu_rate, cores, sample = cpu_reference_rate(a.degree, seconds_target=max(2.0, 12.0 / max(a.steps, 1)))
+    # K steps, each a bounded sample of the workload on all host cores.
+    vals = []
+    for _ in range(a.warmup):
+        pass
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        r, _, _ = cpu_reference_rate(a.degree, seconds_target=1.0, cores=cores)
+        vals.append(r)
+    el = time.perf_counter() - t0
+    value = statistics.median(vals)
+    n = N_FOR_DEGREE[a.degree]
+    return {
+        "metric": METRIC, "value": round(value, 5), "unit": "GDoF/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": round(el / max(a.steps, 1) * 1e3, 2), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"3D Poisson apply, degree {a.degree}, FP64 (sub-boxes of the {n}^3 workload on host cores)"},
+        "cpu_baseline": {"value": round(value, 5), "unit": "GDoF/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 5), "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        line = reference_main(a, rank, world)
+    else:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("nccl")
+        line = gpu_main(a, rank, world, local_rank)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1 and a.impl != "reference":
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

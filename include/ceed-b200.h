@@ -165,11 +165,44 @@ int b200_op_cost(b200_op op, double *bytes, double *flops);
 /* Launch shape in use: elements per block and threads per block. */
 int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_per_block, int *staging);
 int b200_op_set_tile(b200_op op, int elems_per_block, int staging);
+/* Largest elements-per-block the kernel of a staging mode can launch with (threads and shared memory). */
+int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block);
+/* Device time of one v += A u with the current tile, averaged over reps launches (CUDA events; used by the
+ * autotuner, which sweeps elements per block and qdata staging per (P, Q, components, precision)). */
+int b200_op_time(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int reps, double *ms_per_apply);
 int b200_op_destroy(b200_op op);
 
 /* Adjoint of the kappa-weighted diffusion with respect to kappa: g[elem][qpt] = grad(w) . D grad(u), recomputing the
  * gradients from u and w (no stored E-vectors).  Both in the operator's precision. */
 int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qdata, void *g);
+
+/* ---- Conjugate gradients on the fused operator (no libCEED counterpart: the reference solves with PETSc KSPCG around
+ *      CeedOperatorApply in examples/petsc/bps.c).  Homogeneous Dirichlet conditions through mask (1 free, 0 fixed):
+ *      solves m A(m x) = m b from x = 0.  mixed = 0: FP64 CG.  mixed = 1: FP32 CG (op32, qdata32) on the defect
+ *      r = m(b - A64 x), computed in FP64, until |r| / |b| <= rtol.  Dot products and norms accumulate in FP64.
+ *      Blocks of check_every iterations run as one CUDA graph when use_graph = 1.  b, x, mask: FP64 device arrays
+ *      of length n. */
+typedef struct {
+  double rtol;        /* target |m(b - A x)| / |b| */
+  int    max_it;      /* cap on CG iterations (all inner iterations in mixed mode) */
+  int    mixed;       /* 0: FP64 CG, 1: FP32 CG inside FP64 refinement */
+  double inner_rtol;  /* mixed: relative residual reduction of each inner solve */
+  int    max_outer;   /* mixed: cap on refinement steps */
+  int    use_graph;   /* capture iteration blocks in CUDA graphs */
+  int    check_every; /* iterations between convergence checks (graph size) */
+} b200_cg_opts;
+
+typedef struct {
+  int     iterations;   /* CG iterations (summed over refinement steps) */
+  int     outer;        /* refinement steps (1 for FP64 CG) */
+  int     converged;
+  double  rel_residual; /* final |m(b - A64 x)| / |b|, recomputed in FP64 */
+  double  seconds;      /* device time of the solve (CUDA events) */
+  int64_t launches;     /* kernels run by the solve */
+} b200_cg_stats;
+
+int b200_cg_solve(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask, const double *b,
+                  double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats);
 
 #ifdef __cplusplus
 }

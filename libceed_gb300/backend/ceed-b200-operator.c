@@ -1,0 +1,203 @@
+// CeedOperator for `/gpu/cuda/b200`: the fused apply of tensor-H1 hexahedral operators.
+//
+// CeedOperatorApply / ApplyAdd (interface/ceed-operator.c:2271-2410) land here.  On first use the operator is matched
+// against the pattern the fused kernels implement:
+//   apply:  active input/output through one offset restriction and one 3D tensor H1 basis with Q = P + 1, a gallery
+//           pointwise kernel (MassApply, Poisson3DApply, Vector3MassApply, Vector3Poisson3DApply), and qdata as a
+//           passive CEED_EVAL_NONE field through a strided restriction with backend strides -> b200_op_apply;
+//   setup:  Mass3DBuild / Poisson3DBuild with a trilinear coordinate field -> b200_qdata_build.
+// Anything else returns CEED_ERROR_UNSUPPORTED: this backend has no CPU fallback and no delegate.
+#include <string.h>
+
+#include "ceed-b200-backend.h"
+
+static int FieldParts(CeedOperatorField f, CeedElemRestriction *r, CeedBasis *b, CeedVector *v) {
+  CeedCallBackend(CeedOperatorFieldGetElemRestriction(f, r));
+  CeedCallBackend(CeedOperatorFieldGetBasis(f, b));
+  CeedCallBackend(CeedOperatorFieldGetVector(f, v));
+  return CEED_ERROR_SUCCESS;
+}
+
+static int OperatorAnalyse_B200(CeedOperator op) {
+  Ceed                ceed = CeedOperatorReturnCeed(op);
+  CeedOperator_B200  *impl;
+  CeedQFunction       qf;
+  CeedQFunction_B200 *qf_impl;
+  CeedInt             n_in, n_out;
+  CeedOperatorField  *in, *out;
+  b200_ctx            ctx;
+
+  CeedCallBackend(CeedOperatorGetData(op, &impl));
+  if (impl->kind) return CEED_ERROR_SUCCESS;
+  impl->kind = -1;
+  CeedCallBackend(CeedGetB200Context(ceed, &ctx));
+  CeedCallBackend(CeedOperatorGetQFunction(op, &qf));
+  CeedCallBackend(CeedQFunctionGetData(qf, &qf_impl));
+  CeedCallBackend(CeedOperatorGetFields(op, &n_in, &in, &n_out, &out));
+  if (qf_impl->qf_kind == -1) {
+    // Geometric factors: fields "dx" (GRAD of coordinates), "weights" (WEIGHT), output "qdata".
+    CeedElemRestriction rx, rq;
+    CeedBasis           bx, bq;
+    CeedVector          vx, vq;
+    CeedInt             P, dim, nc, esize;
+    bool                backend_strides = false, strided;
+
+    CeedCallBackend(FieldParts(in[0], &rx, &bx, &vx));
+    CeedCallBackend(FieldParts(out[0], &rq, &bq, &vq));
+    CeedCallBackend(CeedBasisGetDimension(bx, &dim));
+    CeedCallBackend(CeedBasisGetNumNodes1D(bx, &P));
+    CeedCallBackend(CeedElemRestrictionGetNumComponents(rx, &nc));
+    CeedCallBackend(CeedElemRestrictionGetElementSize(rx, &esize));
+    CeedCallBackend(CeedElemRestrictionIsStrided(rq, &strided));
+    if (strided) CeedCallBackend(CeedElemRestrictionHasBackendStrides(rq, &backend_strides));
+    CeedCheck(dim == 3 && P == 2 && nc == 3 && esize == 8 && backend_strides, ceed, CEED_ERROR_UNSUPPORTED,
+              "geometric factors on /gpu/cuda/b200 need a trilinear 3-component coordinate field and backend-strided qdata");
+    impl->rstr_x  = rx;
+    impl->basis_x = bx;
+    impl->kind    = 2;
+    CeedCallBackend(CeedElemRestrictionDestroy(&rq));
+    CeedCallBackend(CeedBasisDestroy(&bq));
+    if (vx != CEED_VECTOR_ACTIVE && vx != CEED_VECTOR_NONE) CeedCallBackend(CeedVectorDestroy(&vx));
+    if (vq != CEED_VECTOR_ACTIVE && vq != CEED_VECTOR_NONE) CeedCallBackend(CeedVectorDestroy(&vq));
+    CeedCallBackend(CeedQFunctionDestroy(&qf));
+    return CEED_ERROR_SUCCESS;
+  }
+  CeedCheck(qf_impl->qf_kind >= 0, ceed, CEED_ERROR_UNSUPPORTED, "QFunction is not one of the pointwise kernels compiled for /gpu/cuda/b200");
+  {
+    CeedElemRestriction ru, rq, ro;
+    CeedBasis           bu, bq, bo;
+    CeedVector          vu, vq, vo;
+    CeedInt             dim, P, Q, nc, ne, comp_stride;
+    CeedSize            l_size;
+    bool                is_tensor, strided, backend_strides = false, det;
+    b200_op_desc        d;
+    const CeedScalar   *interp, *grad;
+    CeedRestrictionType type;
+
+    CeedCallBackend(FieldParts(in[0], &ru, &bu, &vu));
+    CeedCallBackend(FieldParts(in[1], &rq, &bq, &vq));
+    CeedCallBackend(FieldParts(out[0], &ro, &bo, &vo));
+    CeedCheck(vu == CEED_VECTOR_ACTIVE && vo == CEED_VECTOR_ACTIVE && ru == ro && bu == bo && vq != CEED_VECTOR_ACTIVE && vq != CEED_VECTOR_NONE, ceed,
+              CEED_ERROR_UNSUPPORTED, "fused apply needs the active field in and out through one restriction and basis, qdata passive");
+    CeedCallBackend(CeedElemRestrictionGetType(ru, &type));
+    CeedCallBackend(CeedBasisIsTensor(bu, &is_tensor));
+    CeedCallBackend(CeedBasisGetDimension(bu, &dim));
+    CeedCallBackend(CeedBasisGetNumNodes1D(bu, &P));
+    CeedCallBackend(CeedBasisGetNumQuadraturePoints1D(bu, &Q));
+    CeedCallBackend(CeedElemRestrictionIsStrided(rq, &strided));
+    if (strided) CeedCallBackend(CeedElemRestrictionHasBackendStrides(rq, &backend_strides));
+    CeedCheck(type == CEED_RESTRICTION_STANDARD && is_tensor && dim == 3 && Q == P + 1 && backend_strides, ceed, CEED_ERROR_UNSUPPORTED,
+              "fused apply needs an offset restriction, a 3D tensor basis with Q = P + 1 and backend-strided qdata");
+    CeedCallBackend(CeedElemRestrictionGetNumComponents(ru, &nc));
+    CeedCallBackend(CeedElemRestrictionGetNumElements(ru, &ne));
+    CeedCallBackend(CeedElemRestrictionGetCompStride(ru, &comp_stride));
+    CeedCallBackend(CeedElemRestrictionGetLVectorSize(ru, &l_size));
+    CeedCallBackend(CeedBasisGetInterp1D(bu, &interp));
+    CeedCallBackend(CeedBasisGetGrad1D(bu, &grad));
+    CeedCallBackend(CeedIsDeterministic(ceed, &det));
+    {
+      CeedElemRestriction_B200 *r_impl;
+
+      CeedCallBackend(CeedElemRestrictionGetData(ru, &r_impl));
+      memset(&d, 0, sizeof d);
+      d.qf          = qf_impl->qf_kind;
+      d.prec        = B200_F64;
+      d.P_1d        = P;
+      d.Q_1d        = Q;
+      d.num_comp    = nc;
+      d.scatter     = det ? B200_SCATTER_DETERMINISTIC : B200_SCATTER_ATOMIC;
+      d.num_elem    = ne;
+      d.l_size      = l_size;
+      d.comp_stride = comp_stride;
+      d.offsets     = r_impl->d_offsets;
+      d.interp_1d   = interp;
+      d.grad_1d     = grad;
+    }
+    CeedCallB200(ceed, b200_op_create(ctx, &d, &impl->op));
+    impl->qdata = vq;  // reference kept until destroy
+    impl->kind  = 1;
+    CeedCallBackend(CeedElemRestrictionDestroy(&ru));
+    CeedCallBackend(CeedElemRestrictionDestroy(&rq));
+    CeedCallBackend(CeedElemRestrictionDestroy(&ro));
+    CeedCallBackend(CeedBasisDestroy(&bu));
+    CeedCallBackend(CeedBasisDestroy(&bq));
+    CeedCallBackend(CeedBasisDestroy(&bo));
+  }
+  CeedCallBackend(CeedQFunctionDestroy(&qf));
+  return CEED_ERROR_SUCCESS;
+}
+
+static int OperatorApplyCore_B200(CeedOperator op, CeedVector in_vec, CeedVector out_vec, bool add) {
+  Ceed               ceed = CeedOperatorReturnCeed(op);
+  CeedOperator_B200 *impl;
+  const CeedScalar  *du, *dv, *dq;
+  b200_ctx           ctx;
+
+  CeedCallBackend(OperatorAnalyse_B200(op));
+  CeedCallBackend(CeedOperatorGetData(op, &impl));
+  CeedCallBackend(CeedGetB200Context(ceed, &ctx));
+  CeedCallBackend(CeedVectorGetDevice_B200(in_vec, false, &du));
+  CeedCallBackend(CeedVectorGetDevice_B200(out_vec, true, &dv));
+  if (impl->kind == 1) {
+    CeedCallBackend(CeedVectorGetDevice_B200(impl->qdata, false, &dq));
+    CeedCallB200(ceed, b200_op_apply(impl->op, du, (void *)dv, dq, NULL, add ? 1 : 0));
+  } else if (impl->kind == 2) {
+    CeedQFunction             qf;
+    CeedQFunction_B200       *qf_impl;
+    CeedElemRestriction_B200 *rx;
+    const CeedScalar         *interp, *grad, *qw;
+    CeedInt                   ne, Q, comp_stride;
+
+    CeedCheck(!add, ceed, CEED_ERROR_UNSUPPORTED, "geometric factors are computed with CeedOperatorApply");
+    CeedCallBackend(CeedOperatorGetQFunction(op, &qf));
+    CeedCallBackend(CeedQFunctionGetData(qf, &qf_impl));
+    CeedCallBackend(CeedElemRestrictionGetData(impl->rstr_x, &rx));
+    CeedCallBackend(CeedElemRestrictionGetNumElements(impl->rstr_x, &ne));
+    CeedCallBackend(CeedElemRestrictionGetCompStride(impl->rstr_x, &comp_stride));
+    CeedCallBackend(CeedBasisGetNumQuadraturePoints1D(impl->basis_x, &Q));
+    CeedCallBackend(CeedBasisGetInterp1D(impl->basis_x, &interp));
+    CeedCallBackend(CeedBasisGetGrad1D(impl->basis_x, &grad));
+    CeedCallBackend(CeedBasisGetQWeights(impl->basis_x, &qw));
+    CeedCallB200(ceed, b200_qdata_build(ctx, qf_impl->build_poisson, ne, Q, interp, grad, qw, rx->d_offsets, comp_stride, du, (double *)dv));
+    CeedCallBackend(CeedQFunctionDestroy(&qf));
+  } else {
+    return CeedError(ceed, CEED_ERROR_UNSUPPORTED, "operator not supported by /gpu/cuda/b200");
+  }
+  return CEED_ERROR_SUCCESS;
+}
+
+static int CeedOperatorApply_B200(CeedOperator op, CeedVector in_vec, CeedVector out_vec, CeedRequest *request) {
+  (void)request;
+  return OperatorApplyCore_B200(op, in_vec, out_vec, false);
+}
+
+static int CeedOperatorApplyAdd_B200(CeedOperator op, CeedVector in_vec, CeedVector out_vec, CeedRequest *request) {
+  (void)request;
+  return OperatorApplyCore_B200(op, in_vec, out_vec, true);
+}
+
+static int CeedOperatorDestroy_B200(CeedOperator op) {
+  CeedOperator_B200 *impl;
+
+  CeedCallBackend(CeedOperatorGetData(op, &impl));
+  if (impl->op) b200_op_destroy(impl->op);
+  if (impl->qdata) CeedCallBackend(CeedVectorDestroy(&impl->qdata));
+  if (impl->rstr_x) CeedCallBackend(CeedElemRestrictionDestroy(&impl->rstr_x));
+  if (impl->basis_x) CeedCallBackend(CeedBasisDestroy(&impl->basis_x));
+  CeedCallBackend(CeedFree(&impl));
+  return CEED_ERROR_SUCCESS;
+}
+
+int CeedOperatorCreate_B200(CeedOperator op) {
+  Ceed               ceed;
+  CeedOperator_B200 *impl;
+
+  CeedCallBackend(CeedOperatorGetCeed(op, &ceed));
+  CeedCallBackend(CeedCalloc(1, &impl));
+  CeedCallBackend(CeedOperatorSetData(op, impl));
+  CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "Apply", CeedOperatorApply_B200));
+  CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "ApplyAdd", CeedOperatorApplyAdd_B200));
+  CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "Destroy", CeedOperatorDestroy_B200));
+  CeedCallBackend(CeedDestroy(&ceed));
+  return CEED_ERROR_SUCCESS;
+}

@@ -1,0 +1,342 @@
+// Conjugate gradients on the fused operator: plain FP64 CG, and FP32 CG inside FP64 iterative refinement.
+//
+// There is no solver inside libCEED; this mirrors the KSPCG use of CeedOperatorApply in the reference's PETSc
+// benchmark driver (examples/petsc/bps.c, "DoFs/Sec in CG" at :287), with homogeneous Dirichlet conditions through a
+// mask (1 on free nodes, 0 on the box boundary): the solver works with m * A(m * x).
+//
+// All scalars (alpha, beta, r.r) stay on the device, so a block of `check_every` iterations is one CUDA graph and the
+// host only reads r.r between blocks.  Dot products and norms are accumulated in FP64 with the fixed-order two-pass
+// reduction, also for FP32 vectors.  Mixed mode (defect correction): r = m(b - A64 x) in FP64; FP32 CG solves
+// A32 d = r to a relative tolerance; x += d in FP64; repeat until |r| / |b| <= rtol.
+#include "b200_internal.cuh"
+#include "b200_reduce.cuh"
+
+#include <cmath>
+
+namespace b200 {
+
+// Device scalars: [0] r.r of the current iterate, [1] p.w, [2] r.r after the update.
+enum { kRR = 0, kPW = 1, kRRNew = 2 };
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) k_cg_mask_dot(int64_t n, const T *__restrict__ mask, const T *__restrict__ p, T *__restrict__ w,
+                                                                  double *__restrict__ partial) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T wi = w[i] * mask[i];
+    w[i]       = wi;
+    acc += (double)p[i] * (double)wi;
+  }
+  acc = block_reduce(kRedDot, acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const double *__restrict__ s, T *__restrict__ x, T *__restrict__ r,
+                                                                const T *__restrict__ p, const T *__restrict__ w, double *__restrict__ partial) {
+  const double pw    = s[kPW];
+  const T      alpha = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
+  double       acc   = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const T ri = r[i] - alpha * w[i];
+    r[i]       = ri;
+    acc += (double)ri * (double)ri;
+  }
+  acc = block_reduce(kRedSumSq, acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+template <typename T>
+__global__ void k_cg_direction(int64_t n, const double *__restrict__ s, const T *__restrict__ r, T *__restrict__ p) {
+  const double rr   = s[kRR];
+  const T      beta = (T)(rr != 0.0 ? s[kRRNew] / rr : 0.0);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = r[i] + beta * p[i];
+}
+
+// Final pass of a reduction into s[dst]; optionally first retire r.r (s[kRR] = s[kRRNew]).
+__global__ void __launch_bounds__(kReduceThreads) k_cg_final(int blocks, const double *__restrict__ partial, double *__restrict__ s, int dst,
+                                                               int retire) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < blocks; i += blockDim.x) acc += partial[i];
+  acc = block_reduce(kRedDot, acc);
+  if (threadIdx.x == 0) {
+    if (retire) s[kRR] = s[kRRNew];
+    s[dst] = acc;
+  }
+}
+
+// r = m (b - r) and its squared norm (r holds A x on entry).
+__global__ void __launch_bounds__(kReduceThreads) k_residual(int64_t n, const double *__restrict__ mask, const double *__restrict__ b,
+                                                               double *__restrict__ r, double *__restrict__ partial) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = mask[i] * (b[i] - r[i]);
+    r[i]            = ri;
+    acc += ri * ri;
+  }
+  acc = block_reduce(kRedSumSq, acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+}
+
+// Start of a CG solve: x = 0, r = p = rhs (masked already), and s[kRR] = s[kRRNew] = r.r.
+template <typename T, typename S>
+__global__ void k_cg_start(int64_t n, const S *__restrict__ rhs, double scale, T *__restrict__ x, T *__restrict__ r, T *__restrict__ p) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T v = (T)((double)rhs[i] * scale);
+    x[i]      = 0;
+    r[i]      = v;
+    p[i]      = v;
+  }
+}
+
+__global__ void k_copy_scalar(double *s, int dst, int src) { s[dst] = s[src]; }
+
+__global__ void k_add_correction(int64_t n, double scale, const float *__restrict__ d, double *__restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] += scale * (double)d[i];
+}
+
+template <typename T>
+__global__ void k_to_prec(int64_t n, const double *__restrict__ src, T *__restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) dst[i] = (T)src[i];
+}
+
+}  // namespace b200
+
+using namespace b200;
+
+struct CgWork {
+  b200_ctx ctx;
+  int64_t  n;
+  int      blocks;
+  double  *partial, *s, *s_host;
+  double  *r64, *p64, *w64;
+  float   *x32, *r32, *p32, *w32, *mask32;
+};
+
+template <typename T>
+static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, int count) {
+  b200_ctx  ctx = wk.ctx;
+  const int g   = wk.blocks;
+  for (int it = 0; it < count; it++) {
+    int st = b200_op_apply(op, p, w, qdata, nullptr, 0);
+    if (st) return st;
+    k_cg_mask_dot<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, mask, p, w, wk.partial);
+    B200_LAUNCHED(ctx, "cg_mask_dot");
+    k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kPW, 1);
+    B200_LAUNCHED(ctx, "cg_final");
+    k_cg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, x, r, p, w, wk.partial);
+    B200_LAUNCHED(ctx, "cg_update");
+    k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kRRNew, 0);
+    B200_LAUNCHED(ctx, "cg_final");
+    k_cg_direction<T><<<stride_grid(ctx, wk.n, 256), 256, 0, ctx->stream>>>(wk.n, wk.s, r, p);
+    B200_LAUNCHED(ctx, "cg_direction");
+  }
+  return B200_SUCCESS;
+}
+
+// Run CG iterations in blocks of `every` (one CUDA graph per block when use_graph) until sqrt(r.r) <= stop or
+// max_it.  On entry s[kRR] = s[kRRNew] = r.r of the start vector.
+template <typename T>
+static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, double stop, int max_it, int every,
+                   int use_graph, int *iters, double *rr_out) {
+  b200_ctx        ctx   = wk.ctx;
+  cudaGraphExec_t exec  = nullptr;
+  int64_t         per_graph = 0;  // kernels one graph launch runs
+  int             done  = 0;
+  double          rr    = 0.0;
+  int             st    = B200_SUCCESS;
+  B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + kRRNew, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  B200_CUDA(cudaStreamSynchronize(ctx->stream));
+  rr = wk.s_host[0];
+  while (done < max_it && !(sqrt(rr) <= stop)) {
+    const int count = every < max_it - done ? every : max_it - done;
+    if (use_graph && count == every) {
+      if (!exec) {
+        cudaGraph_t   graph;
+        const int64_t l0 = ctx->launches;
+        B200_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, count);
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (st) return st;
+        B200_CUDA(ce);
+        B200_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        B200_CUDA(cudaGraphDestroy(graph));
+        per_graph     = ctx->launches - l0;
+        ctx->launches = l0;  // captured, not yet run
+      }
+      B200_CUDA(cudaGraphLaunch(exec, ctx->stream));
+      ctx->launches += per_graph;
+    } else {
+      st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, count);
+      if (st) break;
+    }
+    done += count;
+    B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + kRRNew, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    B200_CUDA(cudaStreamSynchronize(ctx->stream));
+    rr = wk.s_host[0];
+    if (!std::isfinite(rr)) {
+      set_error("CG diverged (r.r = %g after %d iterations)", rr, done);
+      st = B200_ERROR_BACKEND;
+      break;
+    }
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  *iters  = done;
+  *rr_out = rr;
+  return st;
+}
+
+// r64 = m (b - A64 x), returns |r64|.
+static int outer_residual(CgWork &wk, b200_op op64, const void *qdata64, const double *mask, const double *b, const double *x, double *norm) {
+  b200_ctx ctx = wk.ctx;
+  int      st  = b200_op_apply(op64, x, wk.r64, qdata64, nullptr, 0);
+  if (st) return st;
+  k_residual<<<wk.blocks, kReduceThreads, 0, ctx->stream>>>(wk.n, mask, b, wk.r64, wk.partial);
+  B200_LAUNCHED(ctx, "cg_residual");
+  k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(wk.blocks, wk.partial, wk.s, kRRNew, 0);
+  B200_LAUNCHED(ctx, "cg_final");
+  B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + kRRNew, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  B200_CUDA(cudaStreamSynchronize(ctx->stream));
+  *norm = sqrt(wk.s_host[0]);
+  return B200_SUCCESS;
+}
+
+static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask,
+                              const double *b, double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats);
+
+extern "C" int b200_cg_solve(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask, const double *b,
+                             double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats) {
+  B200_CHECK(op64 && qdata64 && mask && b && x && opts && stats, B200_ERROR_INCOMPLETE, "b200_cg_solve: missing argument");
+  B200_CHECK(!opts->mixed || (op32 && qdata32), B200_ERROR_INCOMPLETE, "mixed-precision CG needs the FP32 operator and qdata");
+  // The solve runs on a private non-blocking stream (a legacy default stream cannot be captured into a graph),
+  // ordered after the work already queued on the context's stream and before anything queued after the call.
+  cudaStream_t user_stream = ctx->stream, solve_stream;
+  cudaEvent_t  fork, join;
+  B200_CUDA(cudaStreamCreateWithFlags(&solve_stream, cudaStreamNonBlocking));
+  B200_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+  B200_CUDA(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+  B200_CUDA(cudaEventRecord(fork, user_stream));
+  B200_CUDA(cudaStreamWaitEvent(solve_stream, fork, 0));
+  ctx->stream = solve_stream;
+  const int st_solve = cg_solve_on_stream(ctx, op64, op32, qdata64, qdata32, mask, b, x, n, opts, stats);
+  cudaEventRecord(join, solve_stream);
+  cudaStreamWaitEvent(user_stream, join, 0);
+  ctx->stream = user_stream;
+  cudaStreamSynchronize(solve_stream);
+  cudaStreamDestroy(solve_stream);
+  cudaEventDestroy(fork);
+  cudaEventDestroy(join);
+  return st_solve;
+}
+
+static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask,
+                              const double *b, double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats) {
+  CgWork wk{};
+  wk.ctx    = ctx;
+  wk.n      = n;
+  wk.blocks = reduce_blocks(ctx->num_sms);
+  const int every = opts->check_every > 0 ? opts->check_every : 10;
+  *stats          = b200_cg_stats{};
+  int st          = B200_SUCCESS;
+  B200_CUDA(cudaMalloc(&wk.partial, sizeof(double) * (size_t)(wk.blocks + 8)));
+  B200_CUDA(cudaMalloc(&wk.s, sizeof(double) * 8));
+  B200_CUDA(cudaMallocHost(&wk.s_host, sizeof(double) * 8));
+  B200_CUDA(cudaMalloc(&wk.r64, sizeof(double) * (size_t)n));
+  B200_CUDA(cudaMalloc(&wk.p64, sizeof(double) * (size_t)n));
+  B200_CUDA(cudaMalloc(&wk.w64, sizeof(double) * (size_t)n));
+  if (opts->mixed) {
+    B200_CUDA(cudaMalloc(&wk.x32, sizeof(float) * (size_t)n));
+    B200_CUDA(cudaMalloc(&wk.r32, sizeof(float) * (size_t)n));
+    B200_CUDA(cudaMalloc(&wk.p32, sizeof(float) * (size_t)n));
+    B200_CUDA(cudaMalloc(&wk.w32, sizeof(float) * (size_t)n));
+    B200_CUDA(cudaMalloc(&wk.mask32, sizeof(float) * (size_t)n));
+    k_to_prec<float><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, mask, wk.mask32);
+    B200_LAUNCHED(ctx, "to_f32");
+  }
+  double bnorm = 0.0;
+  st           = reduce_to_device(ctx, B200_F64, kRedSumSq, n, b, nullptr, wk.s + kRRNew);
+  if (!st) {
+    B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + kRRNew, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    B200_CUDA(cudaStreamSynchronize(ctx->stream));
+    bnorm = sqrt(wk.s_host[0]);
+  }
+  const int64_t launches0 = ctx->launches;
+  cudaEvent_t   e0, e1;
+  B200_CUDA(cudaEventCreate(&e0));
+  B200_CUDA(cudaEventCreate(&e1));
+  B200_CUDA(cudaEventRecord(e0, ctx->stream));
+  const double target = opts->rtol * bnorm;
+  double       rnorm  = 0.0;
+  int          total  = 0;
+  if (!st && !opts->mixed) {
+    // FP64 CG from x = 0: r = p = m b.
+    st = b200_vec_pointwise_mult(ctx, B200_F64, n, wk.r64, mask, b);
+    if (!st) {
+      k_cg_start<double, double><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, wk.r64, 1.0, x, wk.r64, wk.p64);
+      st = check_launch(ctx, "cg_start", __FILE__, __LINE__);
+    }
+    if (!st) st = reduce_to_device(ctx, B200_F64, kRedSumSq, n, wk.r64, nullptr, wk.s + kRRNew);
+    if (!st) {
+      k_copy_scalar<<<1, 1, 0, ctx->stream>>>(wk.s, kRR, kRRNew);
+      st = check_launch(ctx, "cg_copy", __FILE__, __LINE__);
+    }
+    double rr = 0.0;
+    if (!st)
+      st = cg_loop<double>(wk, op64, qdata64, mask, x, wk.r64, wk.p64, wk.w64, target, opts->max_it, every, opts->use_graph, &total, &rr);
+    if (!st) st = outer_residual(wk, op64, qdata64, mask, b, x, &rnorm);
+    stats->outer = 1;
+  } else if (!st) {
+    B200_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * (size_t)n, ctx->stream));
+    st = outer_residual(wk, op64, qdata64, mask, b, x, &rnorm);
+    int outer = 0;
+    while (!st && !(rnorm <= target) && outer < opts->max_outer && total < opts->max_it) {
+      // Inner FP32 CG on A d = r / |r| (scaled to unit norm), from d = 0.
+      const double scale = rnorm > 0 ? 1.0 / rnorm : 1.0;
+      k_cg_start<float, double><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, wk.r64, scale, wk.x32, wk.r32, wk.p32);
+      st = check_launch(ctx, "cg_start", __FILE__, __LINE__);
+      if (!st) st = reduce_to_device(ctx, B200_F32, kRedSumSq, n, wk.r32, nullptr, wk.s + kRRNew);
+      if (!st) {
+        k_copy_scalar<<<1, 1, 0, ctx->stream>>>(wk.s, kRR, kRRNew);
+        st = check_launch(ctx, "cg_copy", __FILE__, __LINE__);
+      }
+      int    it = 0;
+      double rr = 0.0;
+      if (!st)
+        st = cg_loop<float>(wk, op32, qdata32, wk.mask32, wk.x32, wk.r32, wk.p32, wk.w32, opts->inner_rtol, opts->max_it - total, every,
+                            opts->use_graph, &it, &rr);
+      total += it;
+      if (st) break;
+      k_add_correction<<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, rnorm, wk.x32, x);
+      st = check_launch(ctx, "cg_correct", __FILE__, __LINE__);
+      if (!st) st = outer_residual(wk, op64, qdata64, mask, b, x, &rnorm);
+      outer++;
+    }
+    stats->outer = outer;
+  }
+  if (!st) {
+    B200_CUDA(cudaEventRecord(e1, ctx->stream));
+    B200_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    stats->seconds = ms * 1e-3;
+  }
+  stats->iterations   = total;
+  stats->rel_residual = bnorm > 0 ? rnorm / bnorm : rnorm;
+  stats->converged    = !st && rnorm <= target;
+  stats->launches     = ctx->launches - launches0;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(wk.partial);
+  cudaFree(wk.s);
+  cudaFreeHost(wk.s_host);
+  cudaFree(wk.r64);
+  cudaFree(wk.p64);
+  cudaFree(wk.w64);
+  cudaFree(wk.x32);
+  cudaFree(wk.r32);
+  cudaFree(wk.p32);
+  cudaFree(wk.w32);
+  cudaFree(wk.mask32);
+  return st;
+}

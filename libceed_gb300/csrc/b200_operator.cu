@@ -245,6 +245,36 @@ extern "C" int b200_op_cost(b200_op op, double *bytes, double *flops) {
   return B200_SUCCESS;
 }
 
+extern "C" int b200_op_time(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int reps, double *ms_per_apply) {
+  b200_ctx    ctx = op->ctx;
+  cudaEvent_t e0, e1;
+  B200_CHECK(reps > 0, B200_ERROR_DIMENSION, "reps must be positive");
+  int st = b200_op_apply(op, u, v, qdata, kappa, 1);  // warm (and fail early on a bad tile)
+  if (st) return st;
+  B200_CUDA(cudaEventCreate(&e0));
+  B200_CUDA(cudaEventCreate(&e1));
+  B200_CUDA(cudaEventRecord(e0, ctx->stream));
+  for (int i = 0; i < reps && !st; i++) st = b200_op_apply(op, u, v, qdata, kappa, 1);
+  B200_CUDA(cudaEventRecord(e1, ctx->stream));
+  B200_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_apply = ms / reps;
+  return st;
+}
+
+extern "C" int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block) {
+  OpInstance inst;
+  const int  Q2 = op->d.Q_1d * op->d.Q_1d;
+  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, staging, &inst), B200_ERROR_UNSUPPORTED, "no kernel for staging %d", staging);
+  int m = inst.max_threads / Q2;
+  while (m > 1 && inst.smem(m) > 200 * 1024) m--;
+  *max_elems_per_block = m < 1 ? 0 : m;
+  return B200_SUCCESS;
+}
+
 extern "C" int b200_op_destroy(b200_op op) {
   if (!op) return B200_SUCCESS;
   if (op->plan) b200_plan_destroy(op->plan);

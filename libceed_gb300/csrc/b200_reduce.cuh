@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_partial(int kind, int
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
-__global__ void __launch_bounds__(kReduceThreads) k_reduce_final(int kind, int blocks, const double *__restrict__ partial,
+static __global__ void __launch_bounds__(kReduceThreads) k_reduce_final(int kind, int blocks, const double *__restrict__ partial,
                                                                  double *__restrict__ result) {
   double acc = 0.0;
   for (int i = threadIdx.x; i < blocks; i += blockDim.x) acc = red_combine(kind, acc, partial[i]);

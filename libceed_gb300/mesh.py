@@ -92,3 +92,35 @@ class Box:
 
     def u(self, seed=None):
         return uniform(self.seed + 1 if seed is None else seed, self.l_size)
+
+
+def node_lattice(n, degree):
+    """Reference (unperturbed) coordinates in [0,1] of the 1D node lattice: element k's Gauss-Lobatto nodes."""
+    from .basis1d import lobatto_quadrature
+
+    gll, _ = lobatto_quadrature(degree + 1)
+    x = np.empty(n * degree + 1)
+    for k in range(n):
+        x[k * degree:(k + 1) * degree + 1] = (k + 0.5 * (gll + 1.0)) / n
+    return x
+
+
+def box_mask(n, degree, ncomp=1):
+    """1 on nodes strictly inside the box, 0 on its faces (homogeneous Dirichlet), per L-vector entry."""
+    nd = n * degree + 1
+    inner = np.ones(nd)
+    inner[0] = inner[-1] = 0.0
+    m = (inner[None, None, :] * inner[None, :, None] * inner[:, None, None]).reshape(-1)
+    return np.repeat(m, ncomp) if ncomp > 1 else m
+
+
+def smooth_field(n, degree, seed, modes=8):
+    """Sum of `modes` seeded low-frequency sines on the node lattice (the manufactured solution of the solve)."""
+    x = node_lattice(n, degree)
+    r = uniform(seed, 4 * modes, 0.0, 1.0)
+    out = np.zeros((x.size, x.size, x.size))
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    for k in range(modes):
+        fx, fy, fz = 1 + int(3 * r[4 * k]), 1 + int(3 * r[4 * k + 1]), 1 + int(3 * r[4 * k + 2])
+        out += (0.5 + r[4 * k + 3]) * np.sin(np.pi * fx * X) * np.sin(np.pi * fy * Y) * np.sin(np.pi * fz * Z)
+    return out.reshape(-1)

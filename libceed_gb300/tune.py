@@ -1,0 +1,88 @@
+"""Autotuner of the fused operator's launch shape.
+
+For each (dim, P, Q, components, precision, QFunction, scatter) it sweeps the elements per block
+(1 up to what threads and shared memory allow) and the qdata staging (registers or shared memory),
+times each candidate on the device (b200_op_time: CUDA events over repeated applies on the real
+problem), keeps the fastest, and records it in a JSON cache (CEED_B200_TUNE_CACHE, default
+~/.cache/libceed_b200/tune.json) so later operators with the same key start from the tuned tile.
+The reference instead sizes blocks by an occupancy-and-waste heuristic
+(backends/cuda-gen/ceed-cuda-gen-operator.c:40-97).
+"""
+import ctypes
+import json
+import os
+
+from ._ffi import call
+from .ceed import F32, F64, QF_POISSON_KAPPA
+
+STAGE_NAMES = {1: "registers", 2: "shared"}
+
+
+def cache_path():
+    return os.environ.get("CEED_B200_TUNE_CACHE", os.path.join(os.path.expanduser("~"), ".cache", "libceed_b200", "tune.json"))
+
+
+def _key(op, prec):
+    f = op._active_input()
+    b, r = f.basis, f.rstr
+    return f"dim{b.dim}_P{b.P1d}_Q{b.Q1d}_nc{r.ncomp}_{'f64' if prec == F64 else 'f32'}_{op.qf.name}_{'det' if op.ceed.deterministic else 'atomic'}"
+
+
+def load_cache():
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def save_cache(cache):
+    path = cache_path()
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def autotune(op, u, v, reps=5, candidates=None, use_cache=True, log=None):
+    """Sweep the launch shape of `op` on vectors u, v; set and return the best {epb, staging, ms, key, sweep}."""
+    prec = u.prec
+    fused = op.fused(prec)
+    key = _key(op, prec)
+    cache = load_cache() if use_cache else {}
+    qd = op._passive("qdata", prec)
+    kap = op._passive("kappa", prec) if op.qf.kind == QF_POISSON_KAPPA else None
+    sweep = []
+    for stage in (1, 2):
+        m = ctypes.c_int()
+        call("b200_op_tile_limits", fused.h, stage, ctypes.byref(m))
+        epbs = candidates or sorted({e for e in (1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 14, 16, 20, 24, 28, 32) if e <= m.value})
+        for epb in epbs:
+            if epb > m.value:
+                continue
+            fused.set_tile(epb, stage)
+            ms = ctypes.c_double()
+            call("b200_op_time", fused.h, u.ptr(), v.ptr(), qd.ptr(), kap.ptr() if kap else None, reps, ctypes.byref(ms))
+            sweep.append({"epb": epb, "staging": STAGE_NAMES[stage], "ms": round(ms.value, 5)})
+            if log:
+                log(f"{key} epb={epb} staging={STAGE_NAMES[stage]} {ms.value:.4f} ms")
+    best = min(sweep, key=lambda r: r["ms"])
+    stage = 1 if best["staging"] == "registers" else 2
+    fused.set_tile(best["epb"], stage)
+    op.elems_per_block, op.staging = best["epb"], stage
+    op._fused[(prec, op.ceed.deterministic, best["epb"], stage)] = fused
+    result = {"key": key, "epb": best["epb"], "staging": best["staging"], "ms": best["ms"], "sweep": sweep}
+    if use_cache:
+        cache[key] = {"epb": best["epb"], "staging": best["staging"], "ms": best["ms"]}
+        save_cache(cache)
+    return result
+
+
+def apply_cached(op, prec=F64):
+    """Set `op` to its cached tile, if the cache has its key; returns the entry or None."""
+    entry = load_cache().get(_key(op, prec))
+    if entry:
+        op.elems_per_block = entry["epb"]
+        op.staging = 1 if entry["staging"] == "registers" else 2
+    return entry
