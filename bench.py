@@ -36,7 +36,7 @@ METRIC = "GDoF/s per operator apply (3D Poisson p=1..8), FP32+refine vs FP64 CG 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--degree", type=int, default=4)
@@ -325,7 +325,7 @@ def run_extras(ceed, lc, mesh, build_poisson, torch, np):
         x = ceed.Vector(box.l_size)
         st = cg_solve(ceed, o64["op"], o64["qdata"], mask, b, x, mixed=mixed, op32=o32["op"], qdata32=o32["qdata"], rtol=1e-10,
                       inner_rtol=1e-4, max_it=20000, use_graph=True, check_every=25)
-        res[tag] = {k: (round(v, 6) if isinstance(v, float) else v) for k, v in st.items()}
+        res[tag] = {k: (float("%.4g" % v) if isinstance(v, float) else v) for k, v in st.items()}
     res["speedup_mixed_over_fp64"] = round(res["fp64_cg"]["seconds"] / res["fp32_refined_cg"]["seconds"], 3)
     res["config"] = f"degree 4, {n}^3 hexes, {box.l_size} DoF, homogeneous Dirichlet, rtol 1e-10, graphs of 25 iterations"
     out["solve"] = res
