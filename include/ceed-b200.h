@@ -201,6 +201,16 @@ typedef struct {
   int64_t launches;     /* kernels run by the solve */
 } b200_cg_stats;
 
+/* ---- Dot product that allocates nothing.  No counterpart in the reference: for callers that cannot allocate device
+ *      memory when they need the reduction (an application allocator that owns all device memory, or a loop that must
+ *      not call cudaMalloc/cudaFree because they can synchronize the device).  Same arithmetic as b200_vec_dot (FP64
+ *      accumulation, fixed order), but the partial sums live in a 128 KiB array inside this library that every GPU
+ *      loading it keeps until exit, and the result goes to `result`, one double in device memory, asynchronously on
+ *      `cuda_stream`; no b200_ctx is needed.  n is limited to 134,217,728 entries (B200_ERROR_DIMENSION beyond).  All
+ *      calls share the array: calls that overlap on the GPU race, so order them on one stream.  The first call on a
+ *      device looks up the array's address with that device current; make it before any stream capture. */
+int b200_vec_dot_static(int prec, int64_t n, const void *x, const void *y, double *result, void *cuda_stream);
+
 int b200_cg_solve(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask, const double *b,
                   double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats);
 
