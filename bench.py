@@ -329,7 +329,65 @@ def run_extras(ceed, lc, mesh, build_poisson, torch, np):
     res["speedup_mixed_over_fp64"] = round(res["fp64_cg"]["seconds"] / res["fp32_refined_cg"]["seconds"], 3)
     res["config"] = f"degree 4, {n}^3 hexes, {box.l_size} DoF, homogeneous Dirichlet, rtol 1e-10, graphs of 25 iterations"
     out["solve"] = res
+    del o64, o32, mask, xv, b
+    torch.cuda.empty_cache()
+    out["vector_autotune"] = run_vector_autotune(ceed, lc, mesh, build_poisson, torch)
+    out["autograd"] = run_autograd(ceed, lc, mesh, torch)
     return out
+
+
+def run_vector_autotune(ceed, lc, mesh, build_poisson, torch):
+    """3-component interlaced vector Poisson and vector mass at degrees 2, 4, 6 (~8M nodes): the autotuner's sweep of
+    elements per block and qdata staging, with the chosen tile and GDoF/s (DoF = 3 x nodes) per (P, Q, ncomp, dtype)."""
+    from libceed_gb300 import tune
+
+    rows = []
+    for p, n in ((2, 99), (4, 50), (6, 33)):
+        box = mesh.Box(n, p, ncomp=3, noise=0.05, seed=5000 + p)
+        for qf in ("Vector3Poisson3DApply", "Vector3MassApply"):
+            for dt in (torch.float32, torch.float64):
+                objs = build_poisson(ceed, box, dtype=dt, qf_name=qf)
+                u = ceed.Vector(box.l_size, dt)
+                u.set_array(box.u())
+                v = ceed.Vector(box.l_size, dt)
+                r = tune.autotune(objs["op"], u, v, reps=3, use_cache=False)
+                rows.append({"qfunction": qf, "degree": p, "P": box.P, "Q": box.Q, "ncomp": 3, "dtype": "f32" if dt == torch.float32 else "f64",
+                             "nodes": box.num_nodes, "dof": box.l_size, "best": {"elems_per_block": r["epb"], "staging": r["staging"]},
+                             "ms": r["ms"], "gdofs": round(box.l_size / r["ms"] / 1e6, 3), "candidates": len(r["sweep"])})
+                del objs, u, v
+                torch.cuda.empty_cache()
+    return rows
+
+
+def run_autograd(ceed, lc, mesh, torch):
+    """Differentiable kappa-weighted diffusion at degree 3, n=42 (2,048,383 DoF), FP32: forward and backward times of
+    L = 1/2 |A(kappa) u - f|^2 with kappa = exp(g), g a 64-mode seeded Gaussian field (sigma 0.5)."""
+    from libceed_gb300.autograd import KappaDiffusion, gaussian_field_kappa, kappa_diffusion
+
+    box = mesh.Box(42, 3, noise=0.05, seed=4242)
+    dop = KappaDiffusion(ceed, box, dtype=torch.float32)
+    kap0 = torch.tensor(gaussian_field_kappa(box, seed=7), device="cuda", dtype=torch.float32)
+    u = torch.tensor(box.u(), device="cuda", dtype=torch.float32, requires_grad=True)
+    kap = kap0.clone().requires_grad_(True)
+    f = torch.tensor(mesh.uniform(4243, box.l_size), device="cuda", dtype=torch.float32)
+    fw, bw = [], []
+    for it in range(8):
+        u.grad = None
+        kap.grad = None
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        loss = 0.5 * torch.sum((kappa_diffusion(u, kap, dop) - f) ** 2)
+        e1.record()
+        loss.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        if it >= 3:
+            fw.append(e0.elapsed_time(e1))
+            bw.append(e1.elapsed_time(e2))
+    return {"config": f"degree 3, 42^3 hexes, {box.l_size} DoF, {box.num_elem * box.Q ** 3} quadrature points, FP32",
+            "forward_ms": round(statistics.median(fw), 4), "backward_ms": round(statistics.median(bw), 4),
+            "note": "forward = fused apply + loss; backward = transpose apply (dL/du) + fused kappa-adjoint kernel (dL/dkappa)"}
 
 
 def reference_main(a, rank, world):

@@ -9,13 +9,22 @@
 // Thread layout ("line" mapping): a team of Q*Q threads per element, team thread (a, b).  In each 1D contraction a
 // thread owns one line of the element tile along the contracted direction: it loads the line from shared memory into
 // registers, applies the 1D matrix (held in the kernel's parameter space, so every FMA reads it as a constant
-// operand) and writes the line back.  The z-direction lines stay in registers across stages.  A block holds
-// `epb` teams; the element tile buffers live in dynamic shared memory.
+// operand) and writes the line back.  The z-direction lines stay in registers across stages.
 //
 // Gradient: collocated, dX = G_c (B u) with G_c = G B^+ (Q x Q); the transpose applies G_c^T then B^T.
-// Staging of qdata: kStageReg prefetches the thread's z-line of qdata into registers at kernel entry (the loads are
-// in flight during the interpolation stages); kStageSmem copies the element's qdata slab into shared memory at entry
-// (reused by all components of a vector field).
+//
+// Even-odd contractions (EO = true): the interpolation matrix of a Lagrange basis on Gauss-Lobatto nodes evaluated at
+// Gauss points is centro-symmetric (B[Q-1-i][P-1-j] = B[i][j]) and the collocated derivative is centro-antisymmetric,
+// so each 1D contraction splits into an even and an odd half on (in[k] +- in[K-1-k]); this removes ~17% (degree 4)
+// to ~30% (degree 8) of the multiply-adds, which is what bounds the FP64 kernels on this GPU.  The host checks the
+// symmetry before choosing an EO kernel.
+//
+// Kernel variants:
+//   k_op_apply<.., kStageReg>  qdata z-line prefetched into registers at entry (loads in flight during interpolation)
+//   k_op_apply<.., kStageSmem> qdata slab of the element copied into shared memory at entry (vector fields reuse it)
+//   k_op_apply_pipe            persistent blocks looping over element batches with a two-deep software pipeline:
+//                              while batch i is computed, batch i+1's qdata streams into a second shared-memory buffer
+//                              (cp.async) and its u values and batch i+2's offsets are loaded into registers.
 #pragma once
 
 #include <cstdint>
@@ -24,19 +33,33 @@
 
 namespace b200 {
 
-enum { kStageReg = 1, kStageSmem = 2 };
+enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3 };
+
+// Even-odd form of a J x K matrix with parity +1 (centro-symmetric) or -1 (centro-antisymmetric).
+template <typename T, int J, int K>
+struct EOMat {
+  static constexpr int Jh = J / 2, Kh = K / 2;
+  T E[Jh * Kh];  // (M[j][k] + M[j][K-1-k]) / 2
+  T O[Jh * Kh];  // (M[j][k] - M[j][K-1-k]) / 2
+  T C[Jh + 1];   // middle input column M[j][Kh] (K odd)
+  T R[Kh + 1];   // middle output row (J odd): even part (parity +1) or odd part (parity -1), then M[Jh][Kh]
+};
 
 template <typename T, int P, int Q>
 struct OpMats {
   T B[Q * P];  // interp, row-major Q x P
   T G[Q * Q];  // collocated gradient, row-major Q x Q
+  EOMat<T, Q, P> Be;   // B   (Q x P), parity +1
+  EOMat<T, P, Q> Bte;  // B^T (P x Q), parity +1
+  EOMat<T, Q, Q> Ge;   // G   (Q x Q), parity -1
+  EOMat<T, Q, Q> Gte;  // G^T (Q x Q), parity -1
 };
 
 template <typename T>
 struct OpArgs {
   int64_t        num_elem;
   int64_t        comp_stride;  // L-vector component stride
-  int            epb;          // elements per block
+  int            epb;          // elements per block (teams per block)
   int            det;          // 1: write the element result to e_out (deterministic scatter follows)
   const int32_t *offsets;
   const T       *u;
@@ -52,13 +75,16 @@ struct QFTraits {
   static constexpr int  nc    = (QF == B200_QF_VECMASS || QF == B200_QF_VECPOISSON) ? 3 : 1;
   static constexpr int  nqd   = grad ? 6 : 1;
   static constexpr bool kappa = QF == B200_QF_POISSON_KAPPA;
+  static constexpr int  nqk   = nqd + (kappa ? 1 : 0);  // staged qdata components, kappa last
 };
 
 template <typename T, int P, int Q, int QF, int STAGE>
 struct OpShape {
   static constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P3 = P * P * P;
-  // Per-team shared memory in elements of T: three Q^3 tile buffers, plus the qdata slab when staged in smem.
-  static constexpr int team_smem = 3 * Q3 + (STAGE == kStageSmem ? (QFTraits<QF>::nqd + (QFTraits<QF>::kappa ? 1 : 0)) * Q3 : 0);
+  // Per-team shared memory in elements of T: three Q^3 tile buffers, plus the qdata slab (smem staging) or two
+  // qdata slabs and the element's offsets (pipelined).
+  static constexpr int team_smem = 3 * Q3 + (STAGE == kStageSmem ? QFTraits<QF>::nqk * Q3 : 0) +
+                                   (STAGE == kStagePipe ? 2 * QFTraits<QF>::nqk * Q3 + (P3 * 4 + (int)sizeof(T) - 1) / (int)sizeof(T) : 0);
 };
 
 // out[j] = sum_k M[j*K + k] in[k], j < J
@@ -85,14 +111,217 @@ __device__ __forceinline__ void mat_apply_t(const T *M, const T (&in)[J], T (&ou
   }
 }
 
-template <typename T, int P, int Q, int QF, int STAGE>
-__global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
-  using TR            = QFTraits<QF>;
-  using SH            = OpShape<T, P, Q, QF, STAGE>;
-  constexpr int Q2    = SH::Q2, Q3 = SH::Q3, P3 = SH::P3, NC = TR::nc, NQD = TR::nqd;
-  constexpr bool GRAD = TR::grad;
-#define IDX(x, y, z) (((z) * Q + (y)) * Q + (x))
+// out = M in through the even-odd form (M is J x K with parity PAR).
+template <typename T, int J, int K, int PAR>
+__device__ __forceinline__ void eo_apply(const EOMat<T, J, K> &M, const T (&in)[K], T (&out)[J]) {
+  constexpr int  Jh = J / 2, Kh = K / 2;
+  constexpr bool Km = K % 2, Jm = J % 2;
+  T              ie[Kh], io[Kh];
+#pragma unroll
+  for (int k = 0; k < Kh; k++) {
+    ie[k] = in[k] + in[K - 1 - k];
+    io[k] = in[k] - in[K - 1 - k];
+  }
+#pragma unroll
+  for (int j = 0; j < Jh; j++) {
+    T e = M.E[j * Kh] * ie[0], o = M.O[j * Kh] * io[0];
+#pragma unroll
+    for (int k = 1; k < Kh; k++) {
+      e = fma(M.E[j * Kh + k], ie[k], e);
+      o = fma(M.O[j * Kh + k], io[k], o);
+    }
+    if constexpr (Km) e = fma(M.C[j], in[Kh], e);
+    out[j]         = e + o;
+    out[J - 1 - j] = PAR > 0 ? e - o : o - e;
+  }
+  if constexpr (Jm) {
+    if constexpr (PAR > 0) {
+      T r = M.R[0] * ie[0];
+#pragma unroll
+      for (int k = 1; k < Kh; k++) r = fma(M.R[k], ie[k], r);
+      if constexpr (Km) r = fma(M.R[Kh], in[Kh], r);
+      out[Jh] = r;
+    } else {
+      T r = M.R[0] * io[0];
+#pragma unroll
+      for (int k = 1; k < Kh; k++) r = fma(M.R[k], io[k], r);
+      out[Jh] = r;
+    }
+  }
+}
 
+template <typename T, int P, int Q, bool EO>
+struct Contract {
+  static __device__ __forceinline__ void interp(const OpMats<T, P, Q> &M, const T (&in)[P], T (&out)[Q]) {
+    if constexpr (EO) eo_apply<T, Q, P, 1>(M.Be, in, out);
+    else mat_apply<T, Q, P>(M.B, in, out);
+  }
+  static __device__ __forceinline__ void interp_t(const OpMats<T, P, Q> &M, const T (&in)[Q], T (&out)[P]) {
+    if constexpr (EO) eo_apply<T, P, Q, 1>(M.Bte, in, out);
+    else mat_apply_t<T, Q, P>(M.B, in, out);
+  }
+  static __device__ __forceinline__ void grad(const OpMats<T, P, Q> &M, const T (&in)[Q], T (&out)[Q]) {
+    if constexpr (EO) eo_apply<T, Q, Q, -1>(M.Ge, in, out);
+    else mat_apply<T, Q, Q>(M.G, in, out);
+  }
+  static __device__ __forceinline__ void grad_t(const OpMats<T, P, Q> &M, const T (&in)[Q], T (&out)[Q]) {
+    if constexpr (EO) eo_apply<T, Q, Q, -1>(M.Gte, in, out);
+    else mat_apply_t<T, Q, Q>(M.G, in, out);
+  }
+};
+
+#define B200_IDX(x, y, z) ((((z) * Q + (y)) * Q) + (x))
+
+// The element pipeline from the gathered tile to the thread's output line.  On entry s0[IDX(x,y,z)] holds the element
+// values (x, y, z < P) and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata
+// component k (kappa already applied) at point (a, b, z).  On exit, threads with a, b < P hold in out[p] the element
+// result at node (p, a, b).  Uses s0, s1, s2 (Q^3 each) and block-wide barriers.
+template <typename T, int P, int Q, int QF, bool EO, typename QD>
+__device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P, Q> &M, int a, int b, QD qd, T (&out)[P]) {
+  using C             = Contract<T, P, Q, EO>;
+  constexpr bool GRAD = QFTraits<QF>::grad;
+  // ---- X interpolation: lines (y, z) < P --------------------------------------------------------------------------
+  if (a < P && b < P) {
+    T in[P], o[Q];
+#pragma unroll
+    for (int k = 0; k < P; k++) in[k] = s0[B200_IDX(k, a, b)];
+    C::interp(M, in, o);
+#pragma unroll
+    for (int j = 0; j < Q; j++) s1[B200_IDX(j, a, b)] = o[j];
+  }
+  __syncthreads();
+  // ---- Y interpolation: lines (x < Q, z < P) ----------------------------------------------------------------------
+  if (b < P) {
+    T in[P], o[Q];
+#pragma unroll
+    for (int k = 0; k < P; k++) in[k] = s1[B200_IDX(a, k, b)];
+    C::interp(M, in, o);
+#pragma unroll
+    for (int j = 0; j < Q; j++) s0[B200_IDX(a, j, b)] = o[j];
+  }
+  __syncthreads();
+  // ---- Z interpolation (+ Z derivative): lines (x, y) --------------------------------------------------------------
+  T U[Q];
+  {
+    T in[P];
+#pragma unroll
+    for (int k = 0; k < P; k++) in[k] = s0[B200_IDX(a, b, k)];
+    C::interp(M, in, U);
+  }
+  if constexpr (GRAD) {
+    T dz[Q];
+#pragma unroll
+    for (int j = 0; j < Q; j++) s1[B200_IDX(a, b, j)] = U[j];
+    C::grad(M, U, dz);
+    __syncthreads();
+    // ---- X and Y derivatives of the interpolated values ------------------------------------------------------------
+    {
+      T in[Q], o[Q];
+#pragma unroll
+      for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(k, a, b)];
+      C::grad(M, in, o);
+#pragma unroll
+      for (int j = 0; j < Q; j++) s0[B200_IDX(j, a, b)] = o[j];
+#pragma unroll
+      for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(a, k, b)];
+      C::grad(M, in, o);
+#pragma unroll
+      for (int j = 0; j < Q; j++) s2[B200_IDX(a, j, b)] = o[j];
+    }
+    __syncthreads();
+    // ---- pointwise QFunction on the z-line (x = a, y = b) ------------------------------------------------------------
+#pragma unroll
+    for (int z = 0; z < Q; z++) {
+      T D[6];
+#pragma unroll
+      for (int k = 0; k < 6; k++) D[k] = qd(k, z);
+      T vg[3];
+      poisson_point(D, s0[B200_IDX(a, b, z)], s2[B200_IDX(a, b, z)], dz[z], vg);
+      s0[B200_IDX(a, b, z)] = vg[0];
+      s2[B200_IDX(a, b, z)] = vg[1];
+      dz[z]                 = vg[2];
+    }
+    __syncthreads();
+    // ---- X derivative, transposed: lines (y, z) --------------------------------------------------------------------
+    {
+      T in[Q], o[Q];
+#pragma unroll
+      for (int k = 0; k < Q; k++) in[k] = s0[B200_IDX(k, a, b)];
+      C::grad_t(M, in, o);
+#pragma unroll
+      for (int j = 0; j < Q; j++) s1[B200_IDX(j, a, b)] = o[j];
+    }
+    __syncthreads();
+    // ---- Y derivative, transposed, accumulated: lines (x, z) ---------------------------------------------------------
+    {
+      T in[Q], o[Q];
+#pragma unroll
+      for (int k = 0; k < Q; k++) in[k] = s2[B200_IDX(a, k, b)];
+      C::grad_t(M, in, o);
+#pragma unroll
+      for (int j = 0; j < Q; j++) s1[B200_IDX(a, j, b)] += o[j];
+    }
+    __syncthreads();
+    // ---- Z derivative transposed + sum, then Z interpolation transposed: lines (x, y) --------------------------------
+    {
+      T w[Q], o[P];
+      C::grad_t(M, dz, w);
+#pragma unroll
+      for (int j = 0; j < Q; j++) w[j] += s1[B200_IDX(a, b, j)];
+      C::interp_t(M, w, o);
+#pragma unroll
+      for (int p = 0; p < P; p++) s0[B200_IDX(a, b, p)] = o[p];
+    }
+  } else {
+    // ---- mass: pointwise product on the z-line, then Z interpolation transposed ----------------------------------------
+    // Each thread reads and rewrites only its own z-line of s0, so no barrier is needed here.
+    T w[Q], o[P];
+#pragma unroll
+    for (int z = 0; z < Q; z++) w[z] = U[z] * qd(0, z);
+    C::interp_t(M, w, o);
+#pragma unroll
+    for (int p = 0; p < P; p++) s0[B200_IDX(a, b, p)] = o[p];
+  }
+  __syncthreads();
+  // ---- Y interpolation transposed: lines (x < Q, z < P) ----------------------------------------------------------------
+  if (b < P) {
+    T in[Q], o[P];
+#pragma unroll
+    for (int k = 0; k < Q; k++) in[k] = s0[B200_IDX(a, k, b)];
+    C::interp_t(M, in, o);
+#pragma unroll
+    for (int p = 0; p < P; p++) s1[B200_IDX(a, p, b)] = o[p];
+  }
+  __syncthreads();
+  // ---- X interpolation transposed: lines (y, z) < P --------------------------------------------------------------------
+  if (a < P && b < P) {
+    T in[Q];
+#pragma unroll
+    for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(k, a, b)];
+    C::interp_t(M, in, out);
+  }
+}
+
+// Scatter the thread's output line (nodes (p, a, b)) of element e, component c.
+template <typename T, int P>
+__device__ __forceinline__ void scatter_line(const OpArgs<T> &args, int64_t e, int c, const int32_t *off_line, int a, int b, const T (&out)[P]) {
+  constexpr int P3   = P * P * P;
+  const int     base = P * (a + P * b);
+  if (args.det) {
+    T *dst = args.e_out + ((int64_t)c * args.num_elem + e) * P3 + base;
+#pragma unroll
+    for (int p = 0; p < P; p++) dst[p] = out[p];
+  } else {
+#pragma unroll
+    for (int p = 0; p < P; p++) atomicAdd(&args.v[(int64_t)off_line[p] + c * args.comp_stride], out[p]);
+  }
+}
+
+template <typename T, int P, int Q, int QF, int STAGE, bool EO>
+__global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
+  using TR         = QFTraits<QF>;
+  using SH         = OpShape<T, P, Q, QF, STAGE>;
+  constexpr int Q2 = SH::Q2, Q3 = SH::Q3, P3 = SH::P3, NC = TR::nc, NQD = TR::nqd;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int     tid = threadIdx.x % Q2, slot = threadIdx.x / Q2;
   const int     a = tid % Q, b = tid / Q;
@@ -101,15 +330,16 @@ __global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
   const int64_t ne     = args.num_elem;
   T *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + Q3, *s2 = s1 + Q3, *sq = s2 + Q3;
 
-  // ---- qdata staging ----------------------------------------------------------------------------------------
-  constexpr int RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1, RK = (STAGE == kStageReg && TR::kappa) ? Q : 1;
-  T rq[RQ][RZ], rk[RK];
+  // ---- qdata staging ------------------------------------------------------------------------------------------------
+  constexpr int RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1;
+  T             rq[RQ][RZ];
   if constexpr (STAGE == kStageReg) {
 #pragma unroll
     for (int z = 0; z < Q; z++) {
+      T kap = T(1);
+      if constexpr (TR::kappa) kap = active ? args.kappa[e * Q3 + B200_IDX(a, b, z)] : T(0);
 #pragma unroll
-      for (int k = 0; k < NQD; k++) rq[k][z] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + IDX(a, b, z)] : T(0);
-      if constexpr (TR::kappa) rk[z] = active ? args.kappa[e * Q3 + IDX(a, b, z)] : T(0);
+      for (int k = 0; k < NQD; k++) rq[k][z] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_IDX(a, b, z)] * kap : T(0);
     }
   } else {
     for (int i = tid; i < NQD * Q3; i += Q2) {
@@ -119,167 +349,140 @@ __global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
     if constexpr (TR::kappa)
       for (int q = tid; q < Q3; q += Q2) sq[NQD * Q3 + q] = active ? args.kappa[e * Q3 + q] : T(0);
   }
+  auto qd = [&](int k, int z) -> T {
+    if constexpr (STAGE == kStageReg) return rq[k][z];
+    else {
+      const int q = B200_IDX(a, b, z);
+      if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];
+      else return sq[k * Q3 + q];
+    }
+  };
 
 #pragma unroll 1
   for (int c = 0; c < NC; c++) {
     if (c > 0) __syncthreads();
-    // ---- gather u into s0[z][y][x] ------------------------------------------------------------------------------
     for (int i = tid; i < P3; i += Q2) {
       const int x = i % P, y = (i / P) % P, z = i / (P * P);
-      s0[IDX(x, y, z)] = active ? args.u[(int64_t)args.offsets[e * P3 + i] + c * args.comp_stride] : T(0);
+      s0[B200_IDX(x, y, z)] = active ? args.u[(int64_t)args.offsets[e * P3 + i] + c * args.comp_stride] : T(0);
     }
     __syncthreads();
-    // ---- X interpolation: lines (y, z) < P ------------------------------------------------------------------------
-    if (a < P && b < P) {
-      T in[P], out[Q];
-#pragma unroll
-      for (int k = 0; k < P; k++) in[k] = s0[IDX(k, a, b)];
-      mat_apply<T, Q, P>(M.B, in, out);
-#pragma unroll
-      for (int j = 0; j < Q; j++) s1[IDX(j, a, b)] = out[j];
-    }
-    __syncthreads();
-    // ---- Y interpolation: lines (x < Q, z < P) --------------------------------------------------------------------
-    if (b < P) {
-      T in[P], out[Q];
-#pragma unroll
-      for (int k = 0; k < P; k++) in[k] = s1[IDX(a, k, b)];
-      mat_apply<T, Q, P>(M.B, in, out);
-#pragma unroll
-      for (int j = 0; j < Q; j++) s0[IDX(a, j, b)] = out[j];
-    }
-    __syncthreads();
-    // ---- Z interpolation (+ Z derivative): lines (x, y) ------------------------------------------------------------
-    T U[Q], dz[GRAD ? Q : 1];
-    {
-      T in[P];
-#pragma unroll
-      for (int k = 0; k < P; k++) in[k] = s0[IDX(a, b, k)];
-      mat_apply<T, Q, P>(M.B, in, U);
-    }
-    if constexpr (GRAD) {
-#pragma unroll
-      for (int j = 0; j < Q; j++) s1[IDX(a, b, j)] = U[j];
-      mat_apply<T, Q, Q>(M.G, U, dz);
-      __syncthreads();
-      // ---- X and Y derivatives of the interpolated values -----------------------------------------------------------
-      {
-        T in[Q], out[Q];
-#pragma unroll
-        for (int k = 0; k < Q; k++) in[k] = s1[IDX(k, a, b)];
-        mat_apply<T, Q, Q>(M.G, in, out);
-#pragma unroll
-        for (int j = 0; j < Q; j++) s0[IDX(j, a, b)] = out[j];
-#pragma unroll
-        for (int k = 0; k < Q; k++) in[k] = s1[IDX(a, k, b)];
-        mat_apply<T, Q, Q>(M.G, in, out);
-#pragma unroll
-        for (int j = 0; j < Q; j++) s2[IDX(a, j, b)] = out[j];
-      }
-      __syncthreads();
-      // ---- pointwise QFunction on the z-line (x = a, y = b) ----------------------------------------------------------
-#pragma unroll
-      for (int z = 0; z < Q; z++) {
-        T D[6];
-#pragma unroll
-        for (int k = 0; k < 6; k++) {
-          if constexpr (STAGE == kStageReg) D[k] = rq[k][z];
-          else D[k] = sq[k * Q3 + IDX(a, b, z)];
-        }
-        if constexpr (TR::kappa) {
-          T kap;
-          if constexpr (STAGE == kStageReg) kap = rk[z];
-          else kap = sq[NQD * Q3 + IDX(a, b, z)];
-#pragma unroll
-          for (int k = 0; k < 6; k++) D[k] *= kap;
-        }
-        T vg[3];
-        poisson_point(D, s0[IDX(a, b, z)], s2[IDX(a, b, z)], dz[z], vg);
-        s0[IDX(a, b, z)] = vg[0];
-        s2[IDX(a, b, z)] = vg[1];
-        dz[z]            = vg[2];
-      }
-      __syncthreads();
-      // ---- X derivative, transposed: lines (y, z) --------------------------------------------------------------------
-      {
-        T in[Q], out[Q];
-#pragma unroll
-        for (int k = 0; k < Q; k++) in[k] = s0[IDX(k, a, b)];
-        mat_apply_t<T, Q, Q>(M.G, in, out);
-#pragma unroll
-        for (int j = 0; j < Q; j++) s1[IDX(j, a, b)] = out[j];
-      }
-      __syncthreads();
-      // ---- Y derivative, transposed, accumulated: lines (x, z) ---------------------------------------------------------
-      {
-        T in[Q], out[Q];
-#pragma unroll
-        for (int k = 0; k < Q; k++) in[k] = s2[IDX(a, k, b)];
-        mat_apply_t<T, Q, Q>(M.G, in, out);
-#pragma unroll
-        for (int j = 0; j < Q; j++) s1[IDX(a, j, b)] += out[j];
-      }
-      __syncthreads();
-      // ---- Z derivative transposed + sum, then Z interpolation transposed: lines (x, y) ---------------------------------
-      {
-        T w[Q], out[P];
-        mat_apply_t<T, Q, Q>(M.G, dz, w);
-#pragma unroll
-        for (int j = 0; j < Q; j++) w[j] += s1[IDX(a, b, j)];
-        mat_apply_t<T, Q, P>(M.B, w, out);
-#pragma unroll
-        for (int p = 0; p < P; p++) s0[IDX(a, b, p)] = out[p];
-      }
-    } else {
-      // ---- mass: pointwise product on the z-line, then Z interpolation transposed ------------------------------------------
-      // Each thread reads and rewrites only its own z-line of s0, so no barrier is needed here.
-      T w[Q], out[P];
-#pragma unroll
-      for (int z = 0; z < Q; z++) {
-        if constexpr (STAGE == kStageReg) w[z] = U[z] * rq[0][z];
-        else w[z] = U[z] * sq[IDX(a, b, z)];
-      }
-      mat_apply_t<T, Q, P>(M.B, w, out);
-#pragma unroll
-      for (int p = 0; p < P; p++) s0[IDX(a, b, p)] = out[p];
-    }
-    __syncthreads();
-    // ---- Y interpolation transposed: lines (x < Q, z < P) ------------------------------------------------------------------
-    if (b < P) {
-      T in[Q], out[P];
-#pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s0[IDX(a, k, b)];
-      mat_apply_t<T, Q, P>(M.B, in, out);
-#pragma unroll
-      for (int p = 0; p < P; p++) s1[IDX(a, p, b)] = out[p];
-    }
-    __syncthreads();
-    // ---- X interpolation transposed and scatter: lines (y, z) < P ----------------------------------------------------------
-    if (a < P && b < P && active) {
-      T in[Q], out[P];
-#pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s1[IDX(k, a, b)];
-      mat_apply_t<T, Q, P>(M.B, in, out);
-      const int base = P * (a + P * b);
-      if (args.det) {
-        T *dst = args.e_out + ((int64_t)c * ne + e) * P3 + base;
-#pragma unroll
-        for (int p = 0; p < P; p++) dst[p] = out[p];
-      } else {
-#pragma unroll
-        for (int p = 0; p < P; p++) atomicAdd(&args.v[(int64_t)args.offsets[e * P3 + base + p] + c * args.comp_stride], out[p]);
-      }
-    }
+    T out[P];
+    op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out);
+    if (a < P && b < P && active) scatter_line<T, P>(args, e, c, args.offsets + e * P3 + P * (a + P * b), a, b, out);
   }
-#undef IDX
+}
+
+// Asynchronous global -> shared copy of one 4- or 8-byte value (completes at cp.async.wait_group).
+template <typename T>
+__device__ __forceinline__ void cp_async_scalar(T *dst, const T *src) {
+  const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T) == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr), "l"(src) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(saddr), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Persistent, software-pipelined variant (one component; even-odd contractions).  Block i handles element batches
+// i, i + gridDim.x, ...; a batch is `epb` consecutive elements, one per team.  Per team: tiles s0..s2, two qdata
+// slabs (qbuf[2][nqk * Q^3]) filled by cp.async one batch ahead, and the batch's offsets (soff) for the scatter.
+template <typename T, int P, int Q, int QF>
+__global__ void k_op_apply_pipe(const OpArgs<T> args, const OpMats<T, P, Q> M) {
+  using TR         = QFTraits<QF>;
+  using SH         = OpShape<T, P, Q, QF, kStagePipe>;
+  constexpr int Q2 = SH::Q2, Q3 = SH::Q3, P3 = SH::P3, NQD = TR::nqd, NQK = TR::nqk;
+  constexpr int PU = (P3 + Q2 - 1) / Q2;  // gathered values per thread
+  static_assert(TR::nc == 1, "the pipelined kernel handles one component");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int     tid = threadIdx.x % Q2, slot = threadIdx.x / Q2;
+  const int     a = tid % Q, b = tid / Q;
+  const int64_t ne     = args.num_elem;
+  const int64_t nbatch = (ne + args.epb - 1) / args.epb;
+  T            *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + Q3, *s2 = s1 + Q3;
+  T            *qbuf[2] = {s2 + Q3, s2 + Q3 + NQK * Q3};
+  int32_t      *soff    = reinterpret_cast<int32_t *>(s2 + Q3 + 2 * NQK * Q3);
+
+  auto elem_of      = [&](int64_t batch) -> int64_t { return batch * args.epb + slot; };
+  auto load_offsets = [&](int64_t batch, int32_t (&o)[PU]) {
+    const int64_t e = elem_of(batch);
+#pragma unroll
+    for (int r = 0; r < PU; r++) {
+      const int i = tid + r * Q2;
+      o[r]        = (batch < nbatch && e < ne && i < P3) ? args.offsets[e * P3 + i] : 0;
+    }
+  };
+  auto load_u = [&](int64_t batch, const int32_t (&o)[PU], T (&uv)[PU]) {
+    const int64_t e = elem_of(batch);
+#pragma unroll
+    for (int r = 0; r < PU; r++) {
+      const int i = tid + r * Q2;
+      uv[r]       = (batch < nbatch && e < ne && i < P3) ? args.u[o[r]] : T(0);
+    }
+  };
+  auto stage_qdata = [&](int64_t batch, T *dst) {
+    const int64_t e = elem_of(batch);
+    if (batch < nbatch && e < ne) {
+      for (int i = tid; i < NQK * Q3; i += Q2) {
+        const int k = i / Q3, q = i % Q3;
+        const T  *src = (TR::kappa && k == NQD) ? args.kappa + e * Q3 + q : args.qdata + ((int64_t)k * ne + e) * Q3 + q;
+        cp_async_scalar(dst + i, src);
+      }
+    }
+    cp_async_commit();
+  };
+
+  int64_t batch = blockIdx.x;
+  int32_t o_cur[PU], o_next[PU];
+  T       u_cur[PU];
+  // Prologue: the first batch's offsets and u, its qdata in flight, and the next batch's offsets.
+  load_offsets(batch, o_cur);
+  load_u(batch, o_cur, u_cur);
+  stage_qdata(batch, qbuf[0]);
+  load_offsets(batch + gridDim.x, o_next);
+  int buf = 0;
+#pragma unroll 1
+  for (; batch < nbatch; batch += gridDim.x) {
+    const int64_t e      = elem_of(batch);
+    const bool    active = e < ne;
+    __syncthreads();  // the previous batch's last reads of s0, s1 and soff are done
+#pragma unroll
+    for (int r = 0; r < PU; r++) {
+      const int i = tid + r * Q2;
+      if (i < P3) {
+        const int x = i % P, y = (i / P) % P, z = i / (P * P);
+        s0[B200_IDX(x, y, z)] = u_cur[r];
+        soff[i]               = o_cur[r];
+      }
+    }
+    // Issue the next batch's loads; they complete while this batch is computed.
+    const int64_t nb = batch + gridDim.x;
+#pragma unroll
+    for (int r = 0; r < PU; r++) o_cur[r] = o_next[r];
+    load_u(nb, o_cur, u_cur);
+    load_offsets(nb + gridDim.x, o_next);
+    stage_qdata(nb, qbuf[buf ^ 1]);
+    cp_async_wait<1>();  // this batch's qdata group has landed (the next one may still be in flight)
+    __syncthreads();
+    const T *sq = qbuf[buf];
+    auto     qd = [&](int k, int z) -> T {
+      const int q = B200_IDX(a, b, z);
+      if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];
+      else return sq[k * Q3 + q];
+    };
+    T out[P];
+    op_stages<T, P, Q, QF, true>(s0, s1, s2, M, a, b, qd, out);
+    if (a < P && b < P && active) scatter_line<T, P>(args, e, 0, soff + P * (a + P * b), a, b, out);
+    buf ^= 1;
+  }
+  cp_async_wait<0>();
 }
 
 // Gradient of the kappa-weighted diffusion with respect to kappa: g[e][q] = grad(w)_q . D_q grad(u)_q, both gradients
 // recomputed from the L-vectors (no stored E-vectors).
 template <typename T, int P, int Q>
 __global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, T *__restrict__ g, const OpMats<T, P, Q> M) {
+  using C          = Contract<T, P, Q, false>;
   constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P3 = P * P * P;
-#define IDX(x, y, z) (((z) * Q + (y)) * Q + (x))
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int     tid = threadIdx.x % Q2, slot = threadIdx.x / Q2;
   const int     a = tid % Q, b = tid / Q;
@@ -294,50 +497,50 @@ __global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, 
     if (pass) __syncthreads();
     for (int i = tid; i < P3; i += Q2) {
       const int x = i % P, y = (i / P) % P, z = i / (P * P);
-      s0[IDX(x, y, z)] = active ? src[args.offsets[e * P3 + i]] : T(0);
+      s0[B200_IDX(x, y, z)] = active ? src[args.offsets[e * P3 + i]] : T(0);
     }
     __syncthreads();
     if (a < P && b < P) {
-      T in[P], out[Q];
+      T in[P], o[Q];
 #pragma unroll
-      for (int k = 0; k < P; k++) in[k] = s0[IDX(k, a, b)];
-      mat_apply<T, Q, P>(M.B, in, out);
+      for (int k = 0; k < P; k++) in[k] = s0[B200_IDX(k, a, b)];
+      C::interp(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s1[IDX(j, a, b)] = out[j];
+      for (int j = 0; j < Q; j++) s1[B200_IDX(j, a, b)] = o[j];
     }
     __syncthreads();
     if (b < P) {
-      T in[P], out[Q];
+      T in[P], o[Q];
 #pragma unroll
-      for (int k = 0; k < P; k++) in[k] = s1[IDX(a, k, b)];
-      mat_apply<T, Q, P>(M.B, in, out);
+      for (int k = 0; k < P; k++) in[k] = s1[B200_IDX(a, k, b)];
+      C::interp(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s0[IDX(a, j, b)] = out[j];
+      for (int j = 0; j < Q; j++) s0[B200_IDX(a, j, b)] = o[j];
     }
     __syncthreads();
     T U[Q], dz[Q];
     {
       T in[P];
 #pragma unroll
-      for (int k = 0; k < P; k++) in[k] = s0[IDX(a, b, k)];
-      mat_apply<T, Q, P>(M.B, in, U);
+      for (int k = 0; k < P; k++) in[k] = s0[B200_IDX(a, b, k)];
+      C::interp(M, in, U);
     }
 #pragma unroll
-    for (int j = 0; j < Q; j++) s1[IDX(a, b, j)] = U[j];
-    mat_apply<T, Q, Q>(M.G, U, dz);
+    for (int j = 0; j < Q; j++) s1[B200_IDX(a, b, j)] = U[j];
+    C::grad(M, U, dz);
     __syncthreads();
     {
-      T in[Q], out[Q];
+      T in[Q], o[Q];
 #pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s1[IDX(k, a, b)];
-      mat_apply<T, Q, Q>(M.G, in, out);
+      for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(k, a, b)];
+      C::grad(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s0[IDX(j, a, b)] = out[j];
+      for (int j = 0; j < Q; j++) s0[B200_IDX(j, a, b)] = o[j];
 #pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s1[IDX(a, k, b)];
-      mat_apply<T, Q, Q>(M.G, in, out);
+      for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(a, k, b)];
+      C::grad(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s2[IDX(a, j, b)] = out[j];
+      for (int j = 0; j < Q; j++) s2[B200_IDX(a, j, b)] = o[j];
     }
     __syncthreads();
     if (pass == 0) {
@@ -345,19 +548,21 @@ __global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, 
       for (int z = 0; z < Q; z++) {
         T D[6];
 #pragma unroll
-        for (int k = 0; k < 6; k++) D[k] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + IDX(a, b, z)] : T(0);
+        for (int k = 0; k < 6; k++) D[k] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_IDX(a, b, z)] : T(0);
         T vg[3];
-        poisson_point(D, s0[IDX(a, b, z)], s2[IDX(a, b, z)], dz[z], vg);
+        poisson_point(D, s0[B200_IDX(a, b, z)], s2[B200_IDX(a, b, z)], dz[z], vg);
         gu[0][z] = vg[0];
         gu[1][z] = vg[1];
         gu[2][z] = vg[2];
       }
     } else if (active) {
 #pragma unroll
-      for (int z = 0; z < Q; z++) g[e * Q3 + IDX(a, b, z)] = s0[IDX(a, b, z)] * gu[0][z] + s2[IDX(a, b, z)] * gu[1][z] + dz[z] * gu[2][z];
+      for (int z = 0; z < Q; z++)
+        g[e * Q3 + B200_IDX(a, b, z)] = s0[B200_IDX(a, b, z)] * gu[0][z] + s2[B200_IDX(a, b, z)] * gu[1][z] + dz[z] * gu[2][z];
     }
   }
-#undef IDX
 }
+
+#undef B200_IDX
 
 }  // namespace b200

@@ -9,6 +9,7 @@
 #include "b200_plan.cuh"
 
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 namespace b200 {
@@ -25,26 +26,36 @@ bool op_table_f32_kappa(int, int, OpInstance *);
 bool kgrad_table_f64(int, OpLauncher *);
 bool kgrad_table_f32(int, OpLauncher *);
 
-bool op_lookup(int prec, int qf, int P, int stage, OpInstance *out) {
+bool op_lookup(int prec, int qf, int P, int variant, OpInstance *out) {
   if (P < kOpPMin || P > kOpPMax) return false;
   if (prec == B200_F64) {
     switch (qf) {
-      case B200_QF_MASS: return op_table_f64_mass(P, stage, out);
-      case B200_QF_POISSON: return op_table_f64_poisson(P, stage, out);
-      case B200_QF_VECMASS: return op_table_f64_vecmass(P, stage, out);
-      case B200_QF_VECPOISSON: return op_table_f64_vecpoisson(P, stage, out);
-      case B200_QF_POISSON_KAPPA: return op_table_f64_kappa(P, stage, out);
+      case B200_QF_MASS: return op_table_f64_mass(P, variant, out);
+      case B200_QF_POISSON: return op_table_f64_poisson(P, variant, out);
+      case B200_QF_VECMASS: return op_table_f64_vecmass(P, variant, out);
+      case B200_QF_VECPOISSON: return op_table_f64_vecpoisson(P, variant, out);
+      case B200_QF_POISSON_KAPPA: return op_table_f64_kappa(P, variant, out);
     }
   } else if (prec == B200_F32) {
     switch (qf) {
-      case B200_QF_MASS: return op_table_f32_mass(P, stage, out);
-      case B200_QF_POISSON: return op_table_f32_poisson(P, stage, out);
-      case B200_QF_VECMASS: return op_table_f32_vecmass(P, stage, out);
-      case B200_QF_VECPOISSON: return op_table_f32_vecpoisson(P, stage, out);
-      case B200_QF_POISSON_KAPPA: return op_table_f32_kappa(P, stage, out);
+      case B200_QF_MASS: return op_table_f32_mass(P, variant, out);
+      case B200_QF_POISSON: return op_table_f32_poisson(P, variant, out);
+      case B200_QF_VECMASS: return op_table_f32_vecmass(P, variant, out);
+      case B200_QF_VECPOISSON: return op_table_f32_vecpoisson(P, variant, out);
+      case B200_QF_POISSON_KAPPA: return op_table_f32_kappa(P, variant, out);
     }
   }
   return false;
+}
+
+// True when M (J x K, row-major) satisfies M[J-1-j][K-1-k] = par * M[j][k] to rounding.
+static bool centro(const double *M, int J, int K, int par) {
+  double scale = 0.0;
+  for (int i = 0; i < J * K; i++) scale = fmax(scale, fabs(M[i]));
+  for (int j = 0; j < J; j++)
+    for (int k = 0; k < K; k++)
+      if (fabs(M[(J - 1 - j) * K + (K - 1 - k)] - par * M[j * K + k]) > 1e-12 * scale) return false;
+  return true;
 }
 
 bool kgrad_lookup(int prec, int P, OpLauncher *out) {
@@ -103,27 +114,67 @@ struct b200_op_s {
   b200_op_desc        d;
   std::vector<double> B, Gc;  // host copies: Q x P interp, Q x Q collocated gradient
   OpInstance          inst;
-  int                 stage, epb;
+  int                 stage, epb, variant;
+  int                 grid;       // persistent variant: blocks
+  bool                symmetric;  // B centro-symmetric and G_c centro-antisymmetric: even-odd kernels apply
   b200_plan           plan;     // deterministic scatter only
   void               *e_work;   // element results for the deterministic scatter, [comp][elem][node]
 };
 
+static int op_variant_of(b200_op op, int stage, int *variant) {
+  const bool eo = op->symmetric;
+  if (stage == kStageReg) *variant = eo ? kVarRegEO : kVarReg;
+  else if (stage == kStageSmem) *variant = eo ? kVarSmemEO : kVarSmem;
+  else if (stage == kStagePipe) {
+    B200_CHECK(eo && op->d.num_comp == 1, B200_ERROR_UNSUPPORTED,
+               "the pipelined kernel needs one component and a centro-symmetric basis (Lagrange on Gauss-Lobatto nodes, Gauss points)");
+    *variant = kVarPipeEO;
+  } else {
+    B200_CHECK(false, B200_ERROR_UNSUPPORTED, "unknown qdata staging %d", stage);
+  }
+  return B200_SUCCESS;
+}
+
+// Default launch shape per precision and QFunction (measured on GB300; the autotuner refines it).
+static void op_default_tile(b200_op op, int *epb, int *stage) {
+  const int Q = op->d.Q_1d;
+  if (*stage <= 0) {
+    if (op->d.num_comp > 1) *stage = kStageSmem;
+    else if (op->symmetric) *stage = kStagePipe;
+    else *stage = op->d.prec == B200_F64 ? kStageSmem : kStageReg;
+  }
+  if (*epb <= 0) {
+    *epb = 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1;
+    if (*stage == kStagePipe) *epb = 128 / (Q * Q) > 0 ? 128 / (Q * Q) : 1;
+  }
+}
+
 static int op_select(b200_op op, int epb, int stage) {
   const int Q = op->d.Q_1d, Q2 = Q * Q;
-  if (stage != kStageReg && stage != kStageSmem) stage = op->d.num_comp > 1 ? kStageSmem : kStageReg;
+  op_default_tile(op, &epb, &stage);
+  int variant;
+  int st = op_variant_of(op, stage, &variant);
+  if (st) return st;
   OpInstance inst;
-  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, stage, &inst), B200_ERROR_UNSUPPORTED,
-             "no compiled fused kernel for prec=%d qf=%d P=%d Q=%d", op->d.prec, op->d.qf, op->d.P_1d, op->d.Q_1d);
+  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, variant, &inst), B200_ERROR_UNSUPPORTED,
+             "no compiled fused kernel for prec=%d qf=%d P=%d Q=%d variant=%d", op->d.prec, op->d.qf, op->d.P_1d, op->d.Q_1d, variant);
   const int max_epb_threads = inst.max_threads / Q2;
   int       max_epb_smem    = 1;
-  while (max_epb_smem < 64 && inst.smem(max_epb_smem + 1) <= 160 * 1024) max_epb_smem++;
-  if (epb <= 0) epb = 256 / Q2 > 0 ? 256 / Q2 : 1;
+  while (max_epb_smem < 64 && inst.smem(max_epb_smem + 1) <= 200 * 1024) max_epb_smem++;
   if (epb > max_epb_threads) epb = max_epb_threads;
   if (epb > max_epb_smem) epb = max_epb_smem;
   B200_CHECK(epb >= 1 && inst.smem(epb) <= 227 * 1024, B200_ERROR_UNSUPPORTED, "fused kernel P=%d does not fit one element per block", op->d.P_1d);
-  op->inst  = inst;
-  op->stage = stage;
-  op->epb   = epb;
+  int grid = 0;
+  if (inst.persistent) {
+    const int occ = inst.occupancy(epb);
+    B200_CHECK(occ >= 1, B200_ERROR_UNSUPPORTED, "pipelined kernel P=%d with %d elements per block cannot be resident", op->d.P_1d, epb);
+    grid = occ * op->ctx->num_sms;
+  }
+  op->inst    = inst;
+  op->stage   = stage;
+  op->epb     = epb;
+  op->variant = variant;
+  op->grid    = grid;
   return B200_SUCCESS;
 }
 
@@ -151,6 +202,7 @@ extern "C" int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *o
     set_error("collocated gradient: interpolation matrix is rank deficient");
     return B200_ERROR_BACKEND;
   }
+  op->symmetric = centro(op->B.data(), Q, P, 1) && centro(op->Gc.data(), Q, Q, -1) && !getenv("CEED_B200_NO_EVEN_ODD");
   int st = op_select(op, d.elems_per_block, d.staging);
   if (!st && d.scatter == B200_SCATTER_DETERMINISTIC && d.num_elem > 0) {
     st = b200_plan_create(ctx, d.num_elem, P * P * P, d.num_comp, d.comp_stride, d.l_size, nullptr, d.offsets, &op->plan);
@@ -188,6 +240,7 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   r.num_elem    = d.num_elem;
   r.comp_stride = d.comp_stride;
   r.epb         = op->epb;
+  r.grid        = op->grid;
   r.det         = d.scatter == B200_SCATTER_DETERMINISTIC;
   r.offsets     = d.offsets;
   r.u           = u;
@@ -268,7 +321,10 @@ extern "C" int b200_op_time(b200_op op, const void *u, void *v, const void *qdat
 extern "C" int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block) {
   OpInstance inst;
   const int  Q2 = op->d.Q_1d * op->d.Q_1d;
-  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, staging, &inst), B200_ERROR_UNSUPPORTED, "no kernel for staging %d", staging);
+  int        variant;
+  *max_elems_per_block = 0;
+  if (op_variant_of(op, staging, &variant)) return B200_SUCCESS;  // staging not available for this operator: no tiles
+  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, variant, &inst), B200_ERROR_UNSUPPORTED, "no kernel for staging %d", staging);
   int m = inst.max_threads / Q2;
   while (m > 1 && inst.smem(m) > 200 * 1024) m--;
   *max_elems_per_block = m < 1 ? 0 : m;

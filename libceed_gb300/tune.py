@@ -15,7 +15,8 @@ import os
 from ._ffi import call
 from .ceed import F32, F64, QF_POISSON_KAPPA
 
-STAGE_NAMES = {1: "registers", 2: "shared"}
+STAGE_NAMES = {1: "registers", 2: "shared", 3: "pipelined"}
+STAGE_CODES = {v: k for k, v in STAGE_NAMES.items()}
 
 
 def cache_path():
@@ -54,7 +55,7 @@ def autotune(op, u, v, reps=5, candidates=None, use_cache=True, log=None):
     qd = op._passive("qdata", prec)
     kap = op._passive("kappa", prec) if op.qf.kind == QF_POISSON_KAPPA else None
     sweep = []
-    for stage in (1, 2):
+    for stage in (1, 2, 3):
         m = ctypes.c_int()
         call("b200_op_tile_limits", fused.h, stage, ctypes.byref(m))
         epbs = candidates or sorted({e for e in (1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 14, 16, 20, 24, 28, 32) if e <= m.value})
@@ -68,7 +69,7 @@ def autotune(op, u, v, reps=5, candidates=None, use_cache=True, log=None):
             if log:
                 log(f"{key} epb={epb} staging={STAGE_NAMES[stage]} {ms.value:.4f} ms")
     best = min(sweep, key=lambda r: r["ms"])
-    stage = 1 if best["staging"] == "registers" else 2
+    stage = STAGE_CODES[best["staging"]]
     fused.set_tile(best["epb"], stage)
     op.elems_per_block, op.staging = best["epb"], stage
     op._fused[(prec, op.ceed.deterministic, best["epb"], stage)] = fused
@@ -84,5 +85,5 @@ def apply_cached(op, prec=F64):
     entry = load_cache().get(_key(op, prec))
     if entry:
         op.elems_per_block = entry["epb"]
-        op.staging = 1 if entry["staging"] == "registers" else 2
+        op.staging = STAGE_CODES[entry["staging"]]
     return entry
