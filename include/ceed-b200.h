@@ -20,8 +20,10 @@
 #ifndef CEED_B200_H
 #define CEED_B200_H
 
+#ifndef __CUDACC_RTC__
 #include <stddef.h>
 #include <stdint.h>
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -171,6 +173,31 @@ int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block);
  * autotuner, which sweeps elements per block and qdata staging per (P, Q, components, precision)). */
 int b200_op_time(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int reps, double *ms_per_apply);
 int b200_op_destroy(b200_op op);
+
+/* ---- QFunctions compiled at run time.  Replaces the NVRTC QFunction path of the reference
+ *      (backends/cuda/ceed-cuda-compile.cpp:70-240, backends/cuda-gen/ceed-cuda-gen-operator-build.cpp:1343-1361): the
+ *      QFunction source ("file.h:Name" of CeedQFunctionCreateInterior, split into path and name) is compiled with NVRTC
+ *      for sm_103a into the fused kernel template, with CeedScalar = the operator's precision.  One active
+ *      one-component field (CEED_EVAL_INTERP or CEED_EVAL_GRAD in and out); every other input is passive with
+ *      CEED_EVAL_NONE through a backend-strided restriction ([comp][elem][qpt]). */
+typedef struct {
+  const char *source_path;   /* file holding the CEED_QFUNCTION */
+  const char *name;          /* its name */
+  int         num_inputs;    /* QFunction inputs, in declaration order (at most 8) */
+  int         input_size[8]; /* field sizes (3 for a GRAD scalar field, 1 for INTERP, qdata sizes ...) */
+  int         active_input;  /* index of the active input */
+  int         eval_in;       /* B200_EVAL_INTERP or B200_EVAL_GRAD */
+  int         eval_out;      /* B200_EVAL_INTERP or B200_EVAL_GRAD (the single output is active) */
+  const char *include_dirs;  /* extra include directories, ':'-separated, or NULL */
+} b200_jit_qfunction;
+
+int b200_op_create_jit(b200_ctx ctx, const b200_op_desc *desc, const b200_jit_qfunction *qf, b200_op *op);
+/* Compile the fused kernel for a QFunction source without loading it (no GPU needed): returns the NVRTC log through
+ * b200_last_error on failure. */
+int b200_jit_compile_check(const b200_jit_qfunction *qf, int prec, int P_1d);
+/* passive: device pointers of the passive inputs in QFunction order (skipping the active one); qf_ctx: the
+ * QFunction context data in device memory, or NULL. */
+int b200_op_apply_jit(b200_op op, const void *u, void *v, const void *const *passive, void *qf_ctx, int add);
 
 /* Adjoint of the kappa-weighted diffusion with respect to kappa: g[elem][qpt] = grad(w) . D grad(u), recomputing the
  * gradients from u and w (no stored E-vectors).  Both in the operator's precision. */

@@ -49,7 +49,17 @@ class CGStats(ctypes.Structure):
     ]
 
 
-_STRUCTS = {"b200_op_desc": OpDesc, "b200_cg_opts": CGOpts, "b200_cg_stats": CGStats}
+class JitQFunction(ctypes.Structure):
+    """b200_jit_qfunction (include/ceed-b200.h)."""
+
+    _fields_ = [
+        ("source_path", ctypes.c_char_p), ("name", ctypes.c_char_p), ("num_inputs", ctypes.c_int),
+        ("input_size", ctypes.c_int * 8), ("active_input", ctypes.c_int), ("eval_in", ctypes.c_int), ("eval_out", ctypes.c_int),
+        ("include_dirs", ctypes.c_char_p),
+    ]
+
+
+_STRUCTS = {"b200_op_desc": OpDesc, "b200_cg_opts": CGOpts, "b200_cg_stats": CGStats, "b200_jit_qfunction": JitQFunction}
 _SCALARS = {
     "int": ctypes.c_int, "int64_t": ctypes.c_int64, "size_t": ctypes.c_size_t, "double": ctypes.c_double,
     "int32_t": ctypes.c_int32,

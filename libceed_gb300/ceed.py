@@ -120,6 +120,12 @@ class Ceed:
     def QFunctionByName(self, name):
         return QFunctionByName(self, name)
 
+    def QFunction(self, vlength, f, source):
+        return QFunction(self, vlength, f, source)
+
+    def QFunctionContext(self):
+        return QFunctionContext(self)
+
     def Operator(self, qf, dqf=None, qdfT=None):
         return Operator(self, qf)
 
@@ -334,6 +340,45 @@ class BasisTensorH1:
             pass
 
 
+class QFunction:
+    """A QFunction given by source (CeedQFunctionCreateInterior): `source` is "path/file.h:Name".  On this backend the
+    source is compiled at run time (NVRTC, sm_103a) into the fused operator kernel; `f` (the host function pointer
+    other backends call) is not used."""
+
+    def __init__(self, ceed, vlength, f, source):
+        if ":" not in source:
+            raise B200Error("CeedQFunctionCreateInterior", 3, f"source {source!r} is not \"path/file.h:Name\"")
+        self.ceed = ceed
+        self.source_path, self.name = source.rsplit(":", 1)
+        self.kind = "jit"
+        self.inputs, self.outputs = [], []
+        self.context = None
+
+    def add_input(self, name, size, emode):
+        self.inputs.append((name, size, emode))
+
+    def add_output(self, name, size, emode):
+        self.outputs.append((name, size, emode))
+
+    def set_context(self, ctx):
+        self.context = ctx
+
+
+class QFunctionContext:
+    """CeedQFunctionContext: bytes copied to device memory for the compiled QFunction."""
+
+    def __init__(self, ceed):
+        self.ceed = ceed
+        self.data = None
+
+    def set_data(self, data, memtype=MEM_HOST, cmode=COPY_VALUES):
+        raw = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+        self.data = torch.from_numpy(raw.copy()).to(self.ceed.device)
+
+    def ptr(self):
+        return _vp(self.data.data_ptr()) if self.data is not None else None
+
+
 class QFunctionByName:
     """A gallery QFunction (CeedQFunctionCreateInteriorByName)."""
 
@@ -373,7 +418,7 @@ class Operator:
         self.staging = 0
 
     def set_field(self, name, rstr, basis, vec):
-        names = [f[0] for f in self.qf.inputs + self.qf.outputs]
+        names = [f[0] for f in list(self.qf.inputs) + list(self.qf.outputs)]
         if name not in names:
             raise B200Error("CeedOperatorSetField", 2, f"QFunction {self.qf.name} has no field {name!r}")
         self.fields[name] = _Field(name, rstr, basis, vec)
@@ -416,8 +461,56 @@ class Operator:
             raise B200Error("CeedOperatorApply", 4, f"field {name!r} precision differs from the active vectors")
         return v
 
+    def _jit_op(self, prec):
+        key = ("jit", prec, self.ceed.deterministic)
+        if key in self._fused:
+            return self._fused[key]
+        from ._ffi import JitQFunction
+
+        qf = self.qf
+        (out_name, out_size, out_mode), = qf.outputs
+        act = [i for i, (n, sz, m) in enumerate(qf.inputs) if isinstance(self.fields[n].vec, str)]
+        if len(act) != 1 or not isinstance(self.fields[out_name].vec, str):
+            raise B200Error("CeedOperatorApply", -2, "compiled QFunctions need exactly one active input and one active output")
+        ai = act[0]
+        f = self.fields[qf.inputs[ai][0]]
+        rstr, basis = f.rstr, f.basis
+        if not isinstance(rstr, ElemRestriction) or not isinstance(basis, BasisTensorH1) or basis.dim != 3 or rstr.ncomp != 1:
+            raise B200Error("CeedOperatorApply", -2, "compiled QFunctions: one-component field on a 3D tensor H1 basis")
+        for i, (n, sz, m) in enumerate(qf.inputs):
+            if i != ai and m != EVAL_NONE:
+                raise B200Error("CeedOperatorApply", -2, f"passive input {n!r} must use CEED_EVAL_NONE")
+        d = OpDesc()
+        d.qf, d.prec, d.P_1d, d.Q_1d, d.num_comp = -1, prec, basis.P1d, basis.Q1d, 1
+        d.scatter = SCATTER_DETERMINISTIC if self.ceed.deterministic else SCATTER_ATOMIC
+        d.num_elem, d.l_size, d.comp_stride = rstr.nelem, rstr.lsize, rstr.compstride
+        d.offsets = rstr.offsets.data_ptr()
+        d.interp_1d = basis.interp1d.ctypes.data
+        d.grad_1d = basis.grad1d.ctypes.data
+        j = JitQFunction()
+        j.source_path, j.name = qf.source_path.encode(), qf.name.encode()
+        j.num_inputs = len(qf.inputs)
+        for i, (n, sz, m) in enumerate(qf.inputs):
+            j.input_size[i] = sz
+        j.active_input = ai
+        j.eval_in, j.eval_out = qf.inputs[ai][2], out_mode
+        j.include_dirs = None
+        h = ctypes.c_void_p()
+        call("b200_op_create_jit", self.ceed._ctx, ctypes.byref(d), ctypes.byref(j), ctypes.byref(h))
+        op = _FusedOp(self.ceed, h, (basis.interp1d, basis.grad1d))
+        op.passive_names = [n for i, (n, sz, m) in enumerate(qf.inputs) if i != ai]
+        self._fused[key] = op
+        return op
+
     def _apply(self, u, v, add):
         kind = self.qf.kind
+        if kind == "jit":
+            op = self._jit_op(u.prec)
+            ptrs = [self._passive(n, u.prec).data.data_ptr() for n in op.passive_names]
+            arr = (ctypes.c_void_p * max(1, len(ptrs)))(*ptrs)
+            ctx = self.qf.context.ptr() if self.qf.context is not None else None
+            call("b200_op_apply_jit", op.h, u.ptr(), v.ptr(), arr, ctx, 1 if add else 0)
+            return
         if isinstance(kind, str):
             return self._build(u, v, add)
         op = self._fused_op(u.prec)

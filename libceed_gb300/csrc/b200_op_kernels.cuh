@@ -27,7 +27,9 @@
 //                              (cp.async) and its u values and batch i+2's offsets are loaded into registers.
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cstdint>
+#endif
 
 #include "b200_pointwise.cuh"
 

@@ -5,6 +5,7 @@
 // occupancy-and-waste heuristic (:40-97).  With the deterministic scatter the fused kernel writes the element results
 // and the inverse-offset plan sums them in a fixed order.
 #include "b200_internal.cuh"
+#include "b200_jit.cuh"
 #include "b200_op_launch.cuh"
 #include "b200_plan.cuh"
 
@@ -13,6 +14,7 @@
 #include <vector>
 
 namespace b200 {
+constexpr int kJitMaxFieldsHost = 8;  // kJitMaxFields of b200_jit_kernel.cuh
 bool op_table_f64_mass(int, int, OpInstance *);
 bool op_table_f64_poisson(int, int, OpInstance *);
 bool op_table_f64_vecmass(int, int, OpInstance *);
@@ -119,6 +121,11 @@ struct b200_op_s {
   bool                symmetric;  // B centro-symmetric and G_c centro-antisymmetric: even-odd kernels apply
   b200_plan           plan;     // deterministic scatter only
   void               *e_work;   // element results for the deterministic scatter, [comp][elem][node]
+  // Run-time compiled QFunction (b200_op_create_jit)
+  bool                jit;
+  cudaKernel_t        jit_kernel;
+  int                 jit_num_passive;
+  std::vector<char>   jit_mats;
 };
 
 static int op_variant_of(b200_op op, int stage, int *variant) {
@@ -229,6 +236,7 @@ extern "C" int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_p
 extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add) {
   b200_ctx            ctx = op->ctx;
   const b200_op_desc &d   = op->d;
+  B200_CHECK(!op->jit, B200_ERROR_INCOMPATIBLE, "operator has a run-time compiled QFunction: use b200_op_apply_jit");
   B200_CHECK(u && v && qdata, B200_ERROR_INCOMPLETE, "b200_op_apply: u, v and qdata are required");
   B200_CHECK(d.qf != B200_QF_POISSON_KAPPA || kappa, B200_ERROR_INCOMPLETE, "kappa-weighted diffusion needs kappa");
   const size_t tsz = d.prec == B200_F64 ? 8 : 4;
@@ -328,6 +336,121 @@ extern "C" int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_b
   int m = inst.max_threads / Q2;
   while (m > 1 && inst.smem(m) > 200 * 1024) m--;
   *max_elems_per_block = m < 1 ? 0 : m;
+  return B200_SUCCESS;
+}
+
+// Shared part of b200_op_create and b200_op_create_jit: validation of the layout fields, collocated gradient, symmetry,
+// deterministic plan.
+static int op_common_init(b200_ctx ctx, const b200_op_desc &d, b200_op op) {
+  B200_CHECK(d.prec == B200_F64 || d.prec == B200_F32, B200_ERROR_UNSUPPORTED, "unknown precision %d", d.prec);
+  B200_CHECK(d.Q_1d == d.P_1d + 1, B200_ERROR_UNSUPPORTED, "fused kernels are compiled for Q_1d = P_1d + 1 (got P=%d, Q=%d)", d.P_1d, d.Q_1d);
+  B200_CHECK(d.P_1d >= kOpPMin && d.P_1d <= kOpPMax, B200_ERROR_UNSUPPORTED, "fused kernels cover P_1d in %d..%d (got %d)", kOpPMin, kOpPMax, d.P_1d);
+  B200_CHECK(d.offsets && d.interp_1d && d.grad_1d, B200_ERROR_INCOMPLETE, "offsets and 1D matrices are required");
+  B200_CHECK(d.scatter == B200_SCATTER_ATOMIC || d.scatter == B200_SCATTER_DETERMINISTIC, B200_ERROR_UNSUPPORTED, "unknown scatter mode %d",
+             d.scatter);
+  op->ctx    = ctx;
+  op->d      = d;
+  op->plan   = nullptr;
+  op->e_work = nullptr;
+  const int P = d.P_1d, Q = d.Q_1d;
+  op->B.assign(d.interp_1d, d.interp_1d + Q * P);
+  op->Gc.assign((size_t)Q * Q, 0.0);
+  B200_CHECK(collocated_grad(P, Q, d.interp_1d, d.grad_1d, op->Gc.data()), B200_ERROR_BACKEND, "collocated gradient: interpolation matrix is rank deficient");
+  op->symmetric = centro(op->B.data(), Q, P, 1) && centro(op->Gc.data(), Q, Q, -1) && !getenv("CEED_B200_NO_EVEN_ODD");
+  if (d.scatter == B200_SCATTER_DETERMINISTIC && d.num_elem > 0) {
+    int st = b200_plan_create(ctx, d.num_elem, P * P * P, d.num_comp, d.comp_stride, d.l_size, nullptr, d.offsets, &op->plan);
+    if (st) return st;
+    const size_t esz = (d.prec == B200_F64 ? 8 : 4) * (size_t)d.num_elem * P * P * P * d.num_comp;
+    B200_CUDA(cudaMalloc(&op->e_work, esz));
+  }
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_create_jit(b200_ctx ctx, const b200_op_desc *desc, const b200_jit_qfunction *qf, b200_op *out) {
+  B200_CHECK(desc && qf && qf->source_path && qf->name, B200_ERROR_INCOMPLETE, "b200_op_create_jit: missing descriptor");
+  B200_CHECK(desc->num_comp == 1, B200_ERROR_UNSUPPORTED, "run-time compiled QFunctions: one-component active field only");
+  B200_CHECK(qf->num_inputs >= 1 && qf->num_inputs <= 8 && qf->active_input >= 0 && qf->active_input < qf->num_inputs, B200_ERROR_DIMENSION,
+             "QFunction inputs: %d with active input %d", qf->num_inputs, qf->active_input);
+  B200_CHECK((qf->eval_in == B200_EVAL_INTERP || qf->eval_in == B200_EVAL_GRAD) && (qf->eval_out == B200_EVAL_INTERP || qf->eval_out == B200_EVAL_GRAD),
+             B200_ERROR_UNSUPPORTED, "active fields must use CEED_EVAL_INTERP or CEED_EVAL_GRAD");
+  B200_CHECK(qf->input_size[qf->active_input] == (qf->eval_in == B200_EVAL_GRAD ? 3 : 1), B200_ERROR_DIMENSION,
+             "active input size %d does not match its eval mode", qf->input_size[qf->active_input]);
+  b200_op op = new b200_op_s();
+  int     st = op_common_init(ctx, *desc, op);
+  if (!st) {
+    JitRequest r;
+    r.source_path  = qf->source_path;
+    r.qf_name      = qf->name;
+    r.prec         = desc->prec;
+    r.P            = desc->P_1d;
+    r.eval_in      = qf->eval_in;
+    r.eval_out     = qf->eval_out;
+    r.eo           = op->symmetric;
+    r.num_inputs   = qf->num_inputs;
+    r.active_input = qf->active_input;
+    for (int i = 0; i < 8; i++) r.input_size[i] = i < qf->num_inputs ? qf->input_size[i] : 0;
+    if (qf->include_dirs) {
+      std::string dirs(qf->include_dirs);
+      size_t      pos = 0;
+      while (pos <= dirs.size()) {
+        const size_t next = dirs.find(':', pos);
+        const auto   item = dirs.substr(pos, next == std::string::npos ? std::string::npos : next - pos);
+        if (!item.empty()) r.include_dirs.push_back(item);
+        if (next == std::string::npos) break;
+        pos = next + 1;
+      }
+    }
+    std::string key;
+    st = jit_compile(r, &op->jit_kernel, &key);
+    if (!st) st = jit_mats_blob(desc->prec, desc->P_1d, op->B.data(), op->Gc.data(), &op->jit_mats);
+  }
+  if (st) {
+    b200_op_destroy(op);
+    return st;
+  }
+  op->jit             = true;
+  op->jit_num_passive = qf->num_inputs - 1;
+  const int Q         = desc->Q_1d;
+  op->epb             = desc->elems_per_block > 0 ? desc->elems_per_block : (256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1);
+  op->stage           = 0;
+  op->variant         = -1;
+  op->grid            = 0;
+  *out                = op;
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void *const *passive, void *qf_ctx, int add) {
+  b200_ctx            ctx = op->ctx;
+  const b200_op_desc &d   = op->d;
+  B200_CHECK(op->jit, B200_ERROR_INCOMPATIBLE, "operator has a compiled pointwise kernel: use b200_op_apply");
+  B200_CHECK(u && v, B200_ERROR_INCOMPLETE, "b200_op_apply_jit: u and v are required");
+  const size_t tsz = d.prec == B200_F64 ? 8 : 4;
+  if (!add && d.scatter == B200_SCATTER_ATOMIC) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
+  if (d.num_elem == 0) return B200_SUCCESS;
+  // Kernel arguments: OpArgs<T>, JitFields<T>, OpMats<T, P, Q> (bytes prepared at create).
+  struct ArgsBlob {
+    int64_t        num_elem, comp_stride;
+    int            epb, det;
+    const int32_t *offsets;
+    const void    *u;
+    void          *v, *e_out;
+    const void    *qdata, *kappa;
+  } a{d.num_elem, d.comp_stride, op->epb, d.scatter == B200_SCATTER_DETERMINISTIC, d.offsets, u, v, op->e_work, nullptr, nullptr};
+  static_assert(sizeof(ArgsBlob) == sizeof(OpArgs<double>), "argument layout");
+  struct FieldsBlob {
+    const void *passive[kJitMaxFieldsHost];
+    void       *ctx;
+  } f{};
+  for (int i = 0; i < op->jit_num_passive && i < kJitMaxFieldsHost; i++) f.passive[i] = passive ? passive[i] : nullptr;
+  f.ctx                 = qf_ctx;
+  void        *params[] = {&a, &f, op->jit_mats.data()};
+  const int    Q = d.Q_1d, Q3 = Q * Q * Q;
+  const size_t smem     = tsz * (size_t)op->epb * 3 * Q3;
+  if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute((const void *)op->jit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = ceil_div(d.num_elem, op->epb);
+  B200_CUDA(cudaLaunchKernel((const void *)op->jit_kernel, dim3((unsigned)grid), dim3(op->epb * Q * Q), params, smem, ctx->stream));
+  B200_LAUNCHED(ctx, "op_apply_jit");
+  if (d.scatter == B200_SCATTER_DETERMINISTIC) return plan_scatter(op->plan, d.prec, op->e_work, v, add);
   return B200_SUCCESS;
 }
 
