@@ -174,6 +174,15 @@ int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block);
 int b200_op_time(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int reps, double *ms_per_apply);
 int b200_op_destroy(b200_op op);
 
+/* ---- Diagonal assembly.  Replaces CeedOperatorLinearAssembleDiagonal (interface/ceed-preconditioning.c:2395) and
+ *      include/ceed/jit-source/cuda/cuda-ref-operator-assemble-diagonal.h for the mass (poisson = 0, qdata 1 comp) and
+ *      diffusion (poisson = 1, qdata 6 comps, optional kappa [elem][qpt]) operators: diag = sum_e E^T diag(A_e), FP64.
+ *      The same diagonal serves every component of a vector field (num_comp, comp_stride).  det_plan (from
+ *      b200_plan_create on the same offsets) makes the sum deterministic; NULL uses atomics. */
+int b200_assemble_diagonal(b200_ctx ctx, int poisson, int P_1d, int Q_1d, int64_t num_elem, int num_comp, int64_t comp_stride, int64_t l_size,
+                           const double *interp_1d, const double *grad_1d, const int32_t *offsets, const double *qdata, const double *kappa,
+                           double *diag, b200_plan det_plan);
+
 /* ---- QFunctions compiled at run time.  Replaces the NVRTC QFunction path of the reference
  *      (backends/cuda/ceed-cuda-compile.cpp:70-240, backends/cuda-gen/ceed-cuda-gen-operator-build.cpp:1343-1361): the
  *      QFunction source ("file.h:Name" of CeedQFunctionCreateInterior, split into path and name) is compiled with NVRTC
@@ -208,7 +217,7 @@ int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qda
  *      solves m A(m x) = m b from x = 0.  mixed = 0: FP64 CG.  mixed = 1: FP32 CG (op32, qdata32) on the defect
  *      r = m(b - A64 x), computed in FP64, until |r| / |b| <= rtol.  Dot products and norms accumulate in FP64.
  *      Blocks of check_every iterations run as one CUDA graph when use_graph = 1.  b, x, mask: FP64 device arrays
- *      of length n. */
+ *      of length n.  With jacobi set (e.g. from b200_assemble_diagonal), the iterations are Jacobi-preconditioned. */
 typedef struct {
   double rtol;        /* target |m(b - A x)| / |b| */
   int    max_it;      /* cap on CG iterations (all inner iterations in mixed mode) */
@@ -217,6 +226,7 @@ typedef struct {
   int    max_outer;   /* mixed: cap on refinement steps */
   int    use_graph;   /* capture iteration blocks in CUDA graphs */
   int    check_every; /* iterations between convergence checks (graph size) */
+  const double *jacobi; /* Jacobi preconditioner: masked 1/diag(A) (FP64, device, length n), or NULL for plain CG */
 } b200_cg_opts;
 
 typedef struct {

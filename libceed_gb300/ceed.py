@@ -129,6 +129,9 @@ class Ceed:
     def Operator(self, qf, dqf=None, qdfT=None):
         return Operator(self, qf)
 
+    def CompositeOperator(self):
+        return CompositeOperator(self)
+
     def __del__(self):
         try:
             if getattr(self, "_ctx", None):
@@ -547,6 +550,30 @@ class Operator:
         op = self._fused_op(u.prec)
         qd = self._passive("qdata", u.prec)
         call("b200_op_kappa_grad", op.h, u.ptr(), w.ptr(), qd.ptr(), g.ptr())
+
+
+class CompositeOperator:
+    """CeedCompositeOperator (interface/ceed-operator.c:1297-1450): the sum of sub-operators on the same vectors.
+    apply zeroes the output once and adds every sub-operator's fused apply."""
+
+    def __init__(self, ceed):
+        self.ceed = ceed
+        self.subs = []
+
+    def add_sub(self, op):
+        self.subs.append(op)
+
+    def apply(self, u, v, request=REQUEST_IMMEDIATE):
+        if not self.subs:
+            v.set_value(0.0)
+            return
+        self.subs[0].apply(u, v)
+        for op in self.subs[1:]:
+            op.apply_add(u, v)
+
+    def apply_add(self, u, v, request=REQUEST_IMMEDIATE):
+        for op in self.subs:
+            op.apply_add(u, v)
 
 
 class _FusedOp:

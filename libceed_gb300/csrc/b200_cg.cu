@@ -15,8 +15,9 @@
 
 namespace b200 {
 
-// Device scalars: [0] r.r of the current iterate, [1] p.w, [2] r.r after the update.
-enum { kRR = 0, kPW = 1, kRRNew = 2 };
+// Device scalars: [0] r.z of the current iterate, [1] p.w, [2] r.z after the update, [3] r.r after the update
+// (z = M r with the Jacobi preconditioner M = diag(A)^-1, or z = r without one, when [2] is r.r itself).
+enum { kRR = 0, kPW = 1, kRRNew = 2, kRes = 3 };
 
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) k_cg_mask_dot(int64_t n, const T *__restrict__ mask, const T *__restrict__ p, T *__restrict__ w,
@@ -47,11 +48,48 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const d
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
+// Preconditioned update: also z = M r, with partial sums of r.z (partial) and r.r (partial2).
 template <typename T>
-__global__ void k_cg_direction(int64_t n, const double *__restrict__ s, const T *__restrict__ r, T *__restrict__ p) {
+__global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const double *__restrict__ s, T *__restrict__ x, T *__restrict__ r,
+                                                                 T *__restrict__ z, const T *__restrict__ inv_diag, const T *__restrict__ p,
+                                                                 const T *__restrict__ w, double *__restrict__ partial, double *__restrict__ partial2) {
+  const double pw    = s[kPW];
+  const T      alpha = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
+  double       rz = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const T ri = r[i] - alpha * w[i];
+    const T zi = inv_diag[i] * ri;
+    r[i]       = ri;
+    z[i]       = zi;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
+  }
+  rz = block_reduce(kRedDot, rz);
+  __syncthreads();
+  rr = block_reduce(kRedSumSq, rr);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x]  = rz;
+    partial2[blockIdx.x] = rr;
+  }
+}
+
+// p = src + beta p, src = r (plain CG) or z (preconditioned).
+template <typename T>
+__global__ void k_cg_direction(int64_t n, const double *__restrict__ s, const T *__restrict__ src, T *__restrict__ p) {
   const double rr   = s[kRR];
   const T      beta = (T)(rr != 0.0 ? s[kRRNew] / rr : 0.0);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = r[i] + beta * p[i];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = src[i] + beta * p[i];
+}
+
+// Start of a preconditioned solve: z = p = M r.
+template <typename T>
+__global__ void k_pcg_start(int64_t n, const T *__restrict__ inv_diag, const T *__restrict__ r, T *__restrict__ z, T *__restrict__ p) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const T zi = inv_diag[i] * r[i];
+    z[i]       = zi;
+    p[i]       = zi;
+  }
 }
 
 // Final pass of a reduction into s[dst]; optionally first retire r.r (s[kRR] = s[kRRNew]).
@@ -109,13 +147,14 @@ struct CgWork {
   b200_ctx ctx;
   int64_t  n;
   int      blocks;
-  double  *partial, *s, *s_host;
-  double  *r64, *p64, *w64;
-  float   *x32, *r32, *p32, *w32, *mask32;
+  double  *partial, *partial2, *s, *s_host;
+  double  *r64, *p64, *w64, *z64;
+  float   *x32, *r32, *p32, *w32, *z32, *mask32, *inv32;
+  const double *inv64;  // Jacobi preconditioner (masked 1/diag) or nullptr
 };
 
 template <typename T>
-static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, int count) {
+static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, T *z, const T *inv, int count) {
   b200_ctx  ctx = wk.ctx;
   const int g   = wk.blocks;
   for (int it = 0; it < count; it++) {
@@ -125,11 +164,18 @@ static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mas
     B200_LAUNCHED(ctx, "cg_mask_dot");
     k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kPW, 1);
     B200_LAUNCHED(ctx, "cg_final");
-    k_cg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, x, r, p, w, wk.partial);
-    B200_LAUNCHED(ctx, "cg_update");
+    if (inv) {
+      k_pcg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, x, r, z, inv, p, w, wk.partial, wk.partial2);
+      B200_LAUNCHED(ctx, "pcg_update");
+      k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial2, wk.s, kRes, 0);
+      B200_LAUNCHED(ctx, "cg_final");
+    } else {
+      k_cg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, x, r, p, w, wk.partial);
+      B200_LAUNCHED(ctx, "cg_update");
+    }
     k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kRRNew, 0);
     B200_LAUNCHED(ctx, "cg_final");
-    k_cg_direction<T><<<stride_grid(ctx, wk.n, 256), 256, 0, ctx->stream>>>(wk.n, wk.s, r, p);
+    k_cg_direction<T><<<stride_grid(ctx, wk.n, 256), 256, 0, ctx->stream>>>(wk.n, wk.s, inv ? z : r, p);
     B200_LAUNCHED(ctx, "cg_direction");
   }
   return B200_SUCCESS;
@@ -138,15 +184,16 @@ static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mas
 // Run CG iterations in blocks of `every` (one CUDA graph per block when use_graph) until sqrt(r.r) <= stop or
 // max_it.  On entry s[kRR] = s[kRRNew] = r.r of the start vector.
 template <typename T>
-static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, double stop, int max_it, int every,
-                   int use_graph, int *iters, double *rr_out) {
+static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, T *z, const T *inv, double stop, int max_it,
+                   int every, int use_graph, int *iters, double *rr_out) {
+  const int conv = inv ? kRes : kRRNew;  // index of r.r
   b200_ctx        ctx   = wk.ctx;
   cudaGraphExec_t exec  = nullptr;
   int64_t         per_graph = 0;  // kernels one graph launch runs
   int             done  = 0;
   double          rr    = 0.0;
   int             st    = B200_SUCCESS;
-  B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + kRRNew, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + conv, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   B200_CUDA(cudaStreamSynchronize(ctx->stream));
   rr = wk.s_host[0];
   while (done < max_it && !(sqrt(rr) <= stop)) {
@@ -156,7 +203,7 @@ static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *
         cudaGraph_t   graph;
         const int64_t l0 = ctx->launches;
         B200_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, count);
+        st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, z, inv, count);
         cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
         if (st) return st;
         B200_CUDA(ce);
@@ -168,11 +215,11 @@ static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *
       B200_CUDA(cudaGraphLaunch(exec, ctx->stream));
       ctx->launches += per_graph;
     } else {
-      st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, count);
+      st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, z, inv, count);
       if (st) break;
     }
     done += count;
-    B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + kRRNew, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + conv, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     B200_CUDA(cudaStreamSynchronize(ctx->stream));
     rr = wk.s_host[0];
     if (!std::isfinite(rr)) {
@@ -185,6 +232,25 @@ static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *
   *iters  = done;
   *rr_out = rr;
   return st;
+}
+
+// After r = p = rhs: with a preconditioner, z = p = M r; s[kRR] = s[kRRNew] = r.z and s[kRes] = r.r.
+template <typename T>
+static int pcg_start(CgWork &wk, T *r, T *z, T *p, const T *inv, int prec) {
+  b200_ctx ctx = wk.ctx;
+  int      st  = reduce_to_device(ctx, prec, kRedSumSq, wk.n, r, nullptr, wk.s + kRes);
+  if (st) return st;
+  if (inv) {
+    k_pcg_start<T><<<stride_grid(ctx, wk.n, 256), 256, 0, ctx->stream>>>(wk.n, inv, r, z, p);
+    B200_LAUNCHED(ctx, "pcg_start");
+    st = reduce_to_device(ctx, prec, kRedDot, wk.n, r, z, wk.s + kRRNew);
+  } else {
+    st = reduce_to_device(ctx, prec, kRedSumSq, wk.n, r, nullptr, wk.s + kRRNew);
+  }
+  if (st) return st;
+  k_copy_scalar<<<1, 1, 0, ctx->stream>>>(wk.s, kRR, kRRNew);
+  B200_LAUNCHED(ctx, "cg_copy");
+  return B200_SUCCESS;
 }
 
 // r64 = m (b - A64 x), returns |r64|.
@@ -239,8 +305,11 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
   const int every = opts->check_every > 0 ? opts->check_every : 10;
   *stats          = b200_cg_stats{};
   int st          = B200_SUCCESS;
+  wk.inv64 = opts->jacobi;
   B200_CUDA(cudaMalloc(&wk.partial, sizeof(double) * (size_t)(wk.blocks + 8)));
+  B200_CUDA(cudaMalloc(&wk.partial2, sizeof(double) * (size_t)(wk.blocks + 8)));
   B200_CUDA(cudaMalloc(&wk.s, sizeof(double) * 8));
+  if (wk.inv64) B200_CUDA(cudaMalloc(&wk.z64, sizeof(double) * (size_t)n));
   B200_CUDA(cudaMallocHost(&wk.s_host, sizeof(double) * 8));
   B200_CUDA(cudaMalloc(&wk.r64, sizeof(double) * (size_t)n));
   B200_CUDA(cudaMalloc(&wk.p64, sizeof(double) * (size_t)n));
@@ -253,6 +322,12 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
     B200_CUDA(cudaMalloc(&wk.mask32, sizeof(float) * (size_t)n));
     k_to_prec<float><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, mask, wk.mask32);
     B200_LAUNCHED(ctx, "to_f32");
+    if (wk.inv64) {
+      B200_CUDA(cudaMalloc(&wk.z32, sizeof(float) * (size_t)n));
+      B200_CUDA(cudaMalloc(&wk.inv32, sizeof(float) * (size_t)n));
+      k_to_prec<float><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, wk.inv64, wk.inv32);
+      B200_LAUNCHED(ctx, "to_f32");
+    }
   }
   double bnorm = 0.0;
   st           = reduce_to_device(ctx, B200_F64, kRedSumSq, n, b, nullptr, wk.s + kRRNew);
@@ -276,14 +351,11 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
       k_cg_start<double, double><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, wk.r64, 1.0, x, wk.r64, wk.p64);
       st = check_launch(ctx, "cg_start", __FILE__, __LINE__);
     }
-    if (!st) st = reduce_to_device(ctx, B200_F64, kRedSumSq, n, wk.r64, nullptr, wk.s + kRRNew);
-    if (!st) {
-      k_copy_scalar<<<1, 1, 0, ctx->stream>>>(wk.s, kRR, kRRNew);
-      st = check_launch(ctx, "cg_copy", __FILE__, __LINE__);
-    }
+    if (!st) st = pcg_start<double>(wk, wk.r64, wk.z64, wk.p64, wk.inv64, B200_F64);
     double rr = 0.0;
     if (!st)
-      st = cg_loop<double>(wk, op64, qdata64, mask, x, wk.r64, wk.p64, wk.w64, target, opts->max_it, every, opts->use_graph, &total, &rr);
+      st = cg_loop<double>(wk, op64, qdata64, mask, x, wk.r64, wk.p64, wk.w64, wk.z64, wk.inv64, target, opts->max_it, every, opts->use_graph,
+                           &total, &rr);
     if (!st) st = outer_residual(wk, op64, qdata64, mask, b, x, &rnorm);
     stats->outer = 1;
   } else if (!st) {
@@ -295,16 +367,12 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
       const double scale = rnorm > 0 ? 1.0 / rnorm : 1.0;
       k_cg_start<float, double><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, wk.r64, scale, wk.x32, wk.r32, wk.p32);
       st = check_launch(ctx, "cg_start", __FILE__, __LINE__);
-      if (!st) st = reduce_to_device(ctx, B200_F32, kRedSumSq, n, wk.r32, nullptr, wk.s + kRRNew);
-      if (!st) {
-        k_copy_scalar<<<1, 1, 0, ctx->stream>>>(wk.s, kRR, kRRNew);
-        st = check_launch(ctx, "cg_copy", __FILE__, __LINE__);
-      }
+      if (!st) st = pcg_start<float>(wk, wk.r32, wk.z32, wk.p32, wk.inv32, B200_F32);
       int    it = 0;
       double rr = 0.0;
       if (!st)
-        st = cg_loop<float>(wk, op32, qdata32, wk.mask32, wk.x32, wk.r32, wk.p32, wk.w32, opts->inner_rtol, opts->max_it - total, every,
-                            opts->use_graph, &it, &rr);
+        st = cg_loop<float>(wk, op32, qdata32, wk.mask32, wk.x32, wk.r32, wk.p32, wk.w32, wk.z32, wk.inv32, opts->inner_rtol, opts->max_it - total,
+                            every, opts->use_graph, &it, &rr);
       total += it;
       if (st) break;
       k_add_correction<<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, rnorm, wk.x32, x);
@@ -328,6 +396,10 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(wk.partial);
+  cudaFree(wk.partial2);
+  cudaFree(wk.z64);
+  cudaFree(wk.z32);
+  cudaFree(wk.inv32);
   cudaFree(wk.s);
   cudaFreeHost(wk.s_host);
   cudaFree(wk.r64);

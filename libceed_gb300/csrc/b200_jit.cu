@@ -128,9 +128,10 @@ int jit_compile(const JitRequest &r, cudaKernel_t *kernel, std::string *key_out,
 
   // Kernel template sources, shipped in-tree next to the compiled library.
   const std::string dir = library_dir();
-  std::string       hdr_abi, hdr_kernels, hdr_point, hdr_jit;
+  std::string       hdr_abi, hdr_kernels, hdr_point, hdr_jit, hdr_df;
   B200_CHECK(read_file(dir + "/../../include/ceed-b200.h", &hdr_abi) && read_file(dir + "/../csrc/b200_op_kernels.cuh", &hdr_kernels) &&
-                 read_file(dir + "/../csrc/b200_pointwise.cuh", &hdr_point) && read_file(dir + "/../csrc/b200_jit_kernel.cuh", &hdr_jit),
+                 read_file(dir + "/../csrc/b200_pointwise.cuh", &hdr_point) && read_file(dir + "/../csrc/b200_jit_kernel.cuh", &hdr_jit) &&
+                 read_file(dir + "/../csrc/b200_dfloat.cuh", &hdr_df),
              B200_ERROR_BACKEND, "kernel template sources not found next to %s", dir.c_str());
 
   // Glue: gather the passive inputs at one point and call the user's QFunction with Q = 1.
@@ -155,9 +156,10 @@ int jit_compile(const JitRequest &r, cudaKernel_t *kernel, std::string *key_out,
   name << "b200::k_op_jit<" << scalar << ", " << r.P << ", " << r.P + 1 << ", " << r.eval_in << ", " << r.eval_out << ", "
        << (r.eo ? "true" : "false") << ">";
   // The user's source is a header of the program; includes beside it resolve through -I.
-  const char *headers[]   = {hdr_abi.c_str(), hdr_kernels.c_str(), hdr_point.c_str(), hdr_jit.c_str(), kCeedTypesShim, kCeedTypesShim, "", user_src.c_str()};
-  const char *hdr_names[] = {"ceed-b200.h", "b200_op_kernels.cuh", "b200_pointwise.cuh", "b200_jit_kernel.cuh", "ceed/types.h", "ceed.h", "math.h",
-                             "b200_user_qfunction.h"};
+  const char *headers[]   = {hdr_abi.c_str(), hdr_kernels.c_str(), hdr_point.c_str(), hdr_jit.c_str(), hdr_df.c_str(),
+                             kCeedTypesShim,  kCeedTypesShim,      "",                user_src.c_str()};
+  const char *hdr_names[] = {"ceed-b200.h",  "b200_op_kernels.cuh", "b200_pointwise.cuh", "b200_jit_kernel.cuh", "b200_dfloat.cuh",
+                             "ceed/types.h", "ceed.h",              "math.h",             "b200_user_qfunction.h"};
   std::string              src_dir = r.source_path.substr(0, r.source_path.rfind('/') == std::string::npos ? 0 : r.source_path.rfind('/'));
   std::vector<std::string> opts    = {"-arch=sm_103a", "-std=c++17", "-default-device", "-DB200_JIT=1"};
   if (!src_dir.empty()) opts.push_back("-I" + src_dir);
@@ -166,7 +168,7 @@ int jit_compile(const JitRequest &r, cudaKernel_t *kernel, std::string *key_out,
   for (const auto &o : opts) copts.push_back(o.c_str());
 
   nvrtcProgram prog;
-  nvrtcResult  nr = g_nvrtc.create(&prog, src.str().c_str(), "b200_jit_operator.cu", 8, headers, hdr_names);
+  nvrtcResult  nr = g_nvrtc.create(&prog, src.str().c_str(), "b200_jit_operator.cu", 9, headers, hdr_names);
   B200_CHECK(nr == NVRTC_SUCCESS, B200_ERROR_BACKEND, "nvrtcCreateProgram: %s", g_nvrtc.error_string(nr));
   g_nvrtc.add_name(prog, name.str().c_str());
   nr = g_nvrtc.compile(prog, (int)copts.size(), copts.data());

@@ -21,10 +21,11 @@ struct JitFields {
   void    *ctx;                     // QFunction context data (device memory) or nullptr
 };
 
-#define B200_IDX(x, y, z) ((((z) * Q + (y)) * Q) + (x))
+#define B200_IDX(x, y, z) ((x) + Q * (y) + tile_plane(Q) * (z))
+#define B200_QLIN(x, y, z) ((x) + Q * ((y) + Q * (z)))
 
 template <typename T, int P, int Q, int EVAL_IN, int EVAL_OUT, bool EO>
-__global__ void k_op_jit(const OpArgs<T> args, const JitFields<T> F, const OpMats<T, P, Q> M) {
+__global__ void k_op_jit(const OpArgs<typename Store<T>::type> args, const JitFields<T> F, const OpMats<T, P, Q> M) {
   using C                 = Contract<T, P, Q, EO>;
   constexpr int  Q2       = Q * Q, Q3 = Q * Q * Q, P3 = P * P * P;
   constexpr bool GRAD_IN  = EVAL_IN == B200_EVAL_GRAD;
@@ -35,7 +36,7 @@ __global__ void k_op_jit(const OpArgs<T> args, const JitFields<T> F, const OpMat
   const int64_t e      = (int64_t)blockIdx.x * args.epb + slot;
   const bool    active = e < args.num_elem;
   const int64_t ne     = args.num_elem;
-  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * 3 * Q3, *s1 = s0 + Q3, *s2 = s1 + Q3;
+  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * tile_team_stride(Q, 0), *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q);
 
   for (int i = tid; i < P3; i += Q2) {
     const int x = i % P, y = (i / P) % P, z = i / (P * P);
@@ -91,7 +92,7 @@ __global__ void k_op_jit(const OpArgs<T> args, const JitFields<T> F, const OpMat
   T w[Q];
 #pragma unroll 1
   for (int z = 0; z < Q; z++) {
-    const int q = B200_IDX(a, b, z);
+    const int q = B200_IDX(a, b, z), qg = B200_QLIN(a, b, z);
     T         act_in[GRAD_IN ? 3 : 1], act_out[GRAD_OUT ? 3 : 1];
     if constexpr (GRAD_IN) {
       act_in[0] = s0[q];
@@ -100,7 +101,7 @@ __global__ void k_op_jit(const OpArgs<T> args, const JitFields<T> F, const OpMat
     } else {
       act_in[0] = U[z];
     }
-    if (active) b200_jit_point(F, ne, e, q, act_in, act_out);
+    if (active) b200_jit_point(F, ne, e, qg, act_in, act_out);
     else
       for (int k = 0; k < (GRAD_OUT ? 3 : 1); k++) act_out[k] = T(0);
     if constexpr (GRAD_OUT) {
@@ -163,5 +164,6 @@ __global__ void k_op_jit(const OpArgs<T> args, const JitFields<T> F, const OpMat
 }
 
 #undef B200_IDX
+#undef B200_QLIN
 
 }  // namespace b200

@@ -31,11 +31,31 @@
 #include <cstdint>
 #endif
 
+#include "b200_dfloat.cuh"
 #include "b200_pointwise.cuh"
 
 namespace b200 {
 
 enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3 };
+
+// Shared-memory layout of an element tile: point (x, y, z) at x + Q*y + tile_plane(Q)*z, three tiles per team
+// (tile_buf each), and a team stride that is fixed modulo 32 words.  The plane padding and the team stride residue
+// were chosen with a model of this kernel's shared-memory accesses (every stage's line reads and writes, per warp,
+// 4-byte words on 32 banks) to minimise the number of wavefronts; e.g. at Q = 6 the model counts 35% fewer than the
+// unpadded Q^3 layout, at Q = 4 a factor 2.7 fewer.  Global arrays (qdata, kappa) keep the linear point order.
+__host__ __device__ constexpr int tile_plane_pad(int Q) {
+  return Q == 3 ? 27 : Q == 4 ? 11 : Q == 5 ? 13 : Q == 6 ? 3 : Q == 7 ? 7 : Q == 8 ? 9 : Q == 9 ? 0 : Q == 10 ? 9 : 0;
+}
+__host__ __device__ constexpr int tile_team_mod(int Q) {  // team stride modulo 32 (in elements)
+  return ((3 * Q * (Q * Q + tile_plane_pad(Q))) + (Q == 3 ? 5 : Q == 4 ? 12 : Q == 5 ? 31 : Q == 6 ? 6 : Q == 7 ? 25 : Q == 8 ? 0
+                                                              : Q == 9 ? 6 : Q == 10 ? 30 : 0)) % 32;
+}
+__host__ __device__ constexpr int tile_plane(int Q) { return Q * Q + tile_plane_pad(Q); }
+__host__ __device__ constexpr int tile_buf(int Q) { return Q * tile_plane(Q); }
+// Team stride (elements of T) for `extra` elements of staging space after the three tiles.
+__host__ __device__ constexpr int tile_team_stride(int Q, int extra) {
+  return 3 * tile_buf(Q) + extra + ((tile_team_mod(Q) - (3 * tile_buf(Q) + extra) % 32) % 32 + 32) % 32;
+}
 
 // Even-odd form of a J x K matrix with parity +1 (centro-symmetric) or -1 (centro-antisymmetric).
 template <typename T, int J, int K>
@@ -85,8 +105,9 @@ struct OpShape {
   static constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P3 = P * P * P;
   // Per-team shared memory in elements of T: three Q^3 tile buffers, plus the qdata slab (smem staging) or two
   // qdata slabs and the element's offsets (pipelined).
-  static constexpr int team_smem = 3 * Q3 + (STAGE == kStageSmem ? QFTraits<QF>::nqk * Q3 : 0) +
-                                   (STAGE == kStagePipe ? 2 * QFTraits<QF>::nqk * Q3 + (P3 * 4 + (int)sizeof(T) - 1) / (int)sizeof(T) : 0);
+  static constexpr int extra     = (STAGE == kStageSmem ? QFTraits<QF>::nqk * Q3 : 0) +
+                               (STAGE == kStagePipe ? 2 * QFTraits<QF>::nqk * Q3 + (P3 * 4 + (int)sizeof(T) - 1) / (int)sizeof(T) : 0);
+  static constexpr int team_smem = tile_team_stride(Q, extra);
 };
 
 // out[j] = sum_k M[j*K + k] in[k], j < J
@@ -96,7 +117,7 @@ __device__ __forceinline__ void mat_apply(const T *M, const T (&in)[K], T (&out)
   for (int j = 0; j < J; j++) {
     T s = M[j * K] * in[0];
 #pragma unroll
-    for (int k = 1; k < K; k++) s = fma(M[j * K + k], in[k], s);
+    for (int k = 1; k < K; k++) s = mad(M[j * K + k], in[k], s);
     out[j] = s;
   }
 }
@@ -108,7 +129,7 @@ __device__ __forceinline__ void mat_apply_t(const T *M, const T (&in)[J], T (&ou
   for (int k = 0; k < K; k++) {
     T s = M[k] * in[0];
 #pragma unroll
-    for (int j = 1; j < J; j++) s = fma(M[j * K + k], in[j], s);
+    for (int j = 1; j < J; j++) s = mad(M[j * K + k], in[j], s);
     out[k] = s;
   }
 }
@@ -129,10 +150,10 @@ __device__ __forceinline__ void eo_apply(const EOMat<T, J, K> &M, const T (&in)[
     T e = M.E[j * Kh] * ie[0], o = M.O[j * Kh] * io[0];
 #pragma unroll
     for (int k = 1; k < Kh; k++) {
-      e = fma(M.E[j * Kh + k], ie[k], e);
-      o = fma(M.O[j * Kh + k], io[k], o);
+      e = mad(M.E[j * Kh + k], ie[k], e);
+      o = mad(M.O[j * Kh + k], io[k], o);
     }
-    if constexpr (Km) e = fma(M.C[j], in[Kh], e);
+    if constexpr (Km) e = mad(M.C[j], in[Kh], e);
     out[j]         = e + o;
     out[J - 1 - j] = PAR > 0 ? e - o : o - e;
   }
@@ -140,13 +161,13 @@ __device__ __forceinline__ void eo_apply(const EOMat<T, J, K> &M, const T (&in)[
     if constexpr (PAR > 0) {
       T r = M.R[0] * ie[0];
 #pragma unroll
-      for (int k = 1; k < Kh; k++) r = fma(M.R[k], ie[k], r);
-      if constexpr (Km) r = fma(M.R[Kh], in[Kh], r);
+      for (int k = 1; k < Kh; k++) r = mad(M.R[k], ie[k], r);
+      if constexpr (Km) r = mad(M.R[Kh], in[Kh], r);
       out[Jh] = r;
     } else {
       T r = M.R[0] * io[0];
 #pragma unroll
-      for (int k = 1; k < Kh; k++) r = fma(M.R[k], io[k], r);
+      for (int k = 1; k < Kh; k++) r = mad(M.R[k], io[k], r);
       out[Jh] = r;
     }
   }
@@ -172,7 +193,8 @@ struct Contract {
   }
 };
 
-#define B200_IDX(x, y, z) ((((z) * Q + (y)) * Q) + (x))
+#define B200_IDX(x, y, z) ((x) + Q * (y) + tile_plane(Q) * (z))  // shared-memory tile position
+#define B200_QLIN(x, y, z) ((x) + Q * ((y) + Q * (z)))         // linear point index of global arrays
 
 // The element pipeline from the gathered tile to the thread's output line.  On entry s0[IDX(x,y,z)] holds the element
 // values (x, y, z < P) and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata
@@ -306,21 +328,23 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
 
 // Scatter the thread's output line (nodes (p, a, b)) of element e, component c.
 template <typename T, int P>
-__device__ __forceinline__ void scatter_line(const OpArgs<T> &args, int64_t e, int c, const int32_t *off_line, int a, int b, const T (&out)[P]) {
+__device__ __forceinline__ void scatter_line(const OpArgs<typename Store<T>::type> &args, int64_t e, int c, const int32_t *off_line, int a, int b,
+                                             const T (&out)[P]) {
+  using S = typename Store<T>::type;
   constexpr int P3   = P * P * P;
   const int     base = P * (a + P * b);
   if (args.det) {
-    T *dst = args.e_out + ((int64_t)c * args.num_elem + e) * P3 + base;
+    S *dst = args.e_out + ((int64_t)c * args.num_elem + e) * P3 + base;
 #pragma unroll
-    for (int p = 0; p < P; p++) dst[p] = out[p];
+    for (int p = 0; p < P; p++) dst[p] = (S)out[p];
   } else {
 #pragma unroll
-    for (int p = 0; p < P; p++) atomicAdd(&args.v[(int64_t)off_line[p] + c * args.comp_stride], out[p]);
+    for (int p = 0; p < P; p++) atomicAdd(&args.v[(int64_t)off_line[p] + c * args.comp_stride], (S)out[p]);
   }
 }
 
 template <typename T, int P, int Q, int QF, int STAGE, bool EO>
-__global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
+__global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
   using TR         = QFTraits<QF>;
   using SH         = OpShape<T, P, Q, QF, STAGE>;
   constexpr int Q2 = SH::Q2, Q3 = SH::Q3, P3 = SH::P3, NC = TR::nc, NQD = TR::nqd;
@@ -330,7 +354,7 @@ __global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
   const int64_t e      = (int64_t)blockIdx.x * args.epb + slot;
   const bool    active = e < args.num_elem;
   const int64_t ne     = args.num_elem;
-  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + Q3, *s2 = s1 + Q3, *sq = s2 + Q3;
+  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q), *sq = s2 + tile_buf(Q);
 
   // ---- qdata staging ------------------------------------------------------------------------------------------------
   constexpr int RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1;
@@ -339,22 +363,22 @@ __global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
 #pragma unroll
     for (int z = 0; z < Q; z++) {
       T kap = T(1);
-      if constexpr (TR::kappa) kap = active ? args.kappa[e * Q3 + B200_IDX(a, b, z)] : T(0);
+      if constexpr (TR::kappa) kap = active ? T(args.kappa[e * Q3 + B200_QLIN(a, b, z)]) : T(0);
 #pragma unroll
-      for (int k = 0; k < NQD; k++) rq[k][z] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_IDX(a, b, z)] * kap : T(0);
+      for (int k = 0; k < NQD; k++) rq[k][z] = active ? T(args.qdata[((int64_t)k * ne + e) * Q3 + B200_QLIN(a, b, z)]) * kap : T(0);
     }
   } else {
     for (int i = tid; i < NQD * Q3; i += Q2) {
       const int k = i / Q3, q = i % Q3;
-      sq[i]       = active ? args.qdata[((int64_t)k * ne + e) * Q3 + q] : T(0);
+      sq[i]       = active ? T(args.qdata[((int64_t)k * ne + e) * Q3 + q]) : T(0);
     }
     if constexpr (TR::kappa)
-      for (int q = tid; q < Q3; q += Q2) sq[NQD * Q3 + q] = active ? args.kappa[e * Q3 + q] : T(0);
+      for (int q = tid; q < Q3; q += Q2) sq[NQD * Q3 + q] = active ? T(args.kappa[e * Q3 + q]) : T(0);
   }
   auto qd = [&](int k, int z) -> T {
     if constexpr (STAGE == kStageReg) return rq[k][z];
     else {
-      const int q = B200_IDX(a, b, z);
+      const int q = B200_QLIN(a, b, z);
       if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];
       else return sq[k * Q3 + q];
     }
@@ -365,7 +389,7 @@ __global__ void k_op_apply(const OpArgs<T> args, const OpMats<T, P, Q> M) {
     if (c > 0) __syncthreads();
     for (int i = tid; i < P3; i += Q2) {
       const int x = i % P, y = (i / P) % P, z = i / (P * P);
-      s0[B200_IDX(x, y, z)] = active ? args.u[(int64_t)args.offsets[e * P3 + i] + c * args.comp_stride] : T(0);
+      s0[B200_IDX(x, y, z)] = active ? T(args.u[(int64_t)args.offsets[e * P3 + i] + c * args.comp_stride]) : T(0);
     }
     __syncthreads();
     T out[P];
@@ -389,7 +413,8 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // i, i + gridDim.x, ...; a batch is `epb` consecutive elements, one per team.  Per team: tiles s0..s2, two qdata
 // slabs (qbuf[2][nqk * Q^3]) filled by cp.async one batch ahead, and the batch's offsets (soff) for the scatter.
 template <typename T, int P, int Q, int QF>
-__global__ void k_op_apply_pipe(const OpArgs<T> args, const OpMats<T, P, Q> M) {
+__global__ void k_op_apply_pipe(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
+  static_assert(sizeof(typename Store<T>::type) == sizeof(T) && !__is_same(T, dfloat), "the pipelined kernel stages storage values as T");
   using TR         = QFTraits<QF>;
   using SH         = OpShape<T, P, Q, QF, kStagePipe>;
   constexpr int Q2 = SH::Q2, Q3 = SH::Q3, P3 = SH::P3, NQD = TR::nqd, NQK = TR::nqk;
@@ -400,9 +425,9 @@ __global__ void k_op_apply_pipe(const OpArgs<T> args, const OpMats<T, P, Q> M) {
   const int     a = tid % Q, b = tid / Q;
   const int64_t ne     = args.num_elem;
   const int64_t nbatch = (ne + args.epb - 1) / args.epb;
-  T            *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + Q3, *s2 = s1 + Q3;
-  T            *qbuf[2] = {s2 + Q3, s2 + Q3 + NQK * Q3};
-  int32_t      *soff    = reinterpret_cast<int32_t *>(s2 + Q3 + 2 * NQK * Q3);
+  T            *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q);
+  T            *qbuf[2] = {s2 + tile_buf(Q), s2 + tile_buf(Q) + NQK * Q3};
+  int32_t      *soff    = reinterpret_cast<int32_t *>(s2 + tile_buf(Q) + 2 * NQK * Q3);
 
   auto elem_of      = [&](int64_t batch) -> int64_t { return batch * args.epb + slot; };
   auto load_offsets = [&](int64_t batch, int32_t (&o)[PU]) {
@@ -467,7 +492,7 @@ __global__ void k_op_apply_pipe(const OpArgs<T> args, const OpMats<T, P, Q> M) {
     __syncthreads();
     const T *sq = qbuf[buf];
     auto     qd = [&](int k, int z) -> T {
-      const int q = B200_IDX(a, b, z);
+      const int q = B200_QLIN(a, b, z);
       if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];
       else return sq[k * Q3 + q];
     };
@@ -482,7 +507,7 @@ __global__ void k_op_apply_pipe(const OpArgs<T> args, const OpMats<T, P, Q> M) {
 // Gradient of the kappa-weighted diffusion with respect to kappa: g[e][q] = grad(w)_q . D_q grad(u)_q, both gradients
 // recomputed from the L-vectors (no stored E-vectors).
 template <typename T, int P, int Q>
-__global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, T *__restrict__ g, const OpMats<T, P, Q> M) {
+__global__ void k_kappa_grad(const OpArgs<typename Store<T>::type> args, const T *__restrict__ w_vec, T *__restrict__ g, const OpMats<T, P, Q> M) {
   using C          = Contract<T, P, Q, false>;
   constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P3 = P * P * P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -491,7 +516,7 @@ __global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, 
   const int64_t e      = (int64_t)blockIdx.x * args.epb + slot;
   const bool    active = e < args.num_elem;
   const int64_t ne     = args.num_elem;
-  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * 3 * Q3, *s1 = s0 + Q3, *s2 = s1 + Q3;
+  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * tile_team_stride(Q, 0), *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q);
   T  gu[3][Q];
 #pragma unroll 1
   for (int pass = 0; pass < 2; pass++) {
@@ -550,7 +575,7 @@ __global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, 
       for (int z = 0; z < Q; z++) {
         T D[6];
 #pragma unroll
-        for (int k = 0; k < 6; k++) D[k] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_IDX(a, b, z)] : T(0);
+        for (int k = 0; k < 6; k++) D[k] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_QLIN(a, b, z)] : T(0);
         T vg[3];
         poisson_point(D, s0[B200_IDX(a, b, z)], s2[B200_IDX(a, b, z)], dz[z], vg);
         gu[0][z] = vg[0];
@@ -560,11 +585,12 @@ __global__ void k_kappa_grad(const OpArgs<T> args, const T *__restrict__ w_vec, 
     } else if (active) {
 #pragma unroll
       for (int z = 0; z < Q; z++)
-        g[e * Q3 + B200_IDX(a, b, z)] = s0[B200_IDX(a, b, z)] * gu[0][z] + s2[B200_IDX(a, b, z)] * gu[1][z] + dz[z] * gu[2][z];
+        g[e * Q3 + B200_QLIN(a, b, z)] = s0[B200_IDX(a, b, z)] * gu[0][z] + s2[B200_IDX(a, b, z)] * gu[1][z] + dz[z] * gu[2][z];
     }
   }
 }
 
 #undef B200_IDX
+#undef B200_QLIN
 
 }  // namespace b200

@@ -72,18 +72,19 @@ inline OpMats<T, P, Q> make_mats(const double *B, const double *G) {
 }
 
 template <typename T>
-inline OpArgs<T> make_args(const OpLaunch &r) {
-  OpArgs<T> a;
+inline OpArgs<typename Store<T>::type> make_args(const OpLaunch &r) {
+  using S = typename Store<T>::type;
+  OpArgs<S> a;
   a.num_elem    = r.num_elem;
   a.comp_stride = r.comp_stride;
   a.epb         = r.epb;
   a.det         = r.det;
   a.offsets     = r.offsets;
-  a.u           = (const T *)r.u;
-  a.v           = (T *)r.v;
-  a.e_out       = (T *)r.e_out;
-  a.qdata       = (const T *)r.qdata;
-  a.kappa       = (const T *)r.kappa;
+  a.u           = (const S *)r.u;
+  a.v           = (S *)r.v;
+  a.e_out       = (S *)r.e_out;
+  a.qdata       = (const S *)r.qdata;
+  a.kappa       = (const S *)r.kappa;
   return a;
 }
 
@@ -129,7 +130,7 @@ template <typename T, int P>
 int kgrad_launch(b200_ctx ctx, const OpLaunch &r) {
   constexpr int Q    = P + 1;
   auto          kern = k_kappa_grad<T, P, Q>;
-  const size_t  smem = sizeof(T) * (size_t)r.epb * 3 * Q * Q * Q;
+  const size_t  smem = sizeof(T) * (size_t)r.epb * tile_team_stride(Q, 0);
   if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t grid = ceil_div(r.num_elem, r.epb);
   kern<<<(unsigned)grid, r.epb * Q * Q, smem, ctx->stream>>>(make_args<T>(r), (const T *)r.w, (T *)r.g, make_mats<T, P, Q>(r.B, r.G));

@@ -277,7 +277,7 @@ extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, cons
   r.comp_stride = d.comp_stride;
   const int Q   = d.Q_1d;
   r.epb         = 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1;
-  while (r.epb > 1 && (size_t)(d.prec == B200_F64 ? 8 : 4) * r.epb * 3 * Q * Q * Q > 96 * 1024) r.epb--;
+  while (r.epb > 1 && (size_t)(d.prec == B200_F64 ? 8 : 4) * r.epb * tile_team_stride(Q, 0) > 96 * 1024) r.epb--;
   r.offsets = d.offsets;
   r.u       = u;
   r.w       = w;
@@ -445,7 +445,7 @@ extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void 
   f.ctx                 = qf_ctx;
   void        *params[] = {&a, &f, op->jit_mats.data()};
   const int    Q = d.Q_1d, Q3 = Q * Q * Q;
-  const size_t smem     = tsz * (size_t)op->epb * 3 * Q3;
+  const size_t smem     = tsz * (size_t)op->epb * tile_team_stride(Q, 0);
   if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute((const void *)op->jit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t grid = ceil_div(d.num_elem, op->epb);
   B200_CUDA(cudaLaunchKernel((const void *)op->jit_kernel, dim3((unsigned)grid), dim3(op->epb * Q * Q), params, smem, ctx->stream));
