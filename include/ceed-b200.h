@@ -14,7 +14,9 @@
  *   offsets    int32 [elem][node], device memory
  *   1D matrices row-major Q x P (interp, grad) and Q x Q (collocated grad), host memory at create time
  *
- * Precision: B200_F64 kernels compute in double; B200_F32 kernels compute and accumulate in float.
+ * Precision: B200_F64 kernels compute in double; B200_F32 kernels compute and accumulate in float.  B200_F64X (fused
+ * operator only) reads and writes double vectors but computes in float-float (a pair of floats, ~48-bit significand)
+ * on the FP32 pipes; its results agree with B200_F64 to ~1e-13 relative.  Every other call treats B200_F64X as B200_F64.
  * Every call is asynchronous on the context's stream unless it returns a host value.
  */
 #ifndef CEED_B200_H
@@ -41,7 +43,7 @@ enum {
   B200_ERROR_BACKEND      = -1,
 };
 
-enum { B200_F64 = 0, B200_F32 = 1 };
+enum { B200_F64 = 0, B200_F32 = 1, B200_F64X = 2 };
 enum { B200_NOTRANSPOSE = 0, B200_TRANSPOSE = 1 };                                             /* CeedTransposeMode */
 enum { B200_EVAL_NONE = 0, B200_EVAL_INTERP = 1, B200_EVAL_GRAD = 2, B200_EVAL_WEIGHT = 16 }; /* CeedEvalMode */
 enum { B200_NORM_1 = 0, B200_NORM_2 = 1, B200_NORM_MAX = 2 };                                  /* CeedNormType */
@@ -144,7 +146,7 @@ int b200_qdata_build(b200_ctx ctx, int poisson, int64_t num_elem, int Q_1d, cons
  *      kernel -> transposes -> scatter in one kernel per element batch. -------------------------------------------- */
 typedef struct {
   int            qf;          /* B200_QF_* */
-  int            prec;        /* B200_F64 or B200_F32 */
+  int            prec;        /* B200_F64, B200_F32 or B200_F64X (mass and Poisson, centro-symmetric bases) */
   int            P_1d, Q_1d;  /* Q_1d = P_1d + 1 for the compiled kernels, P_1d in 2..9 */
   int            num_comp;    /* 1, or 3 for the vector QFunctions */
   int            scatter;     /* B200_SCATTER_ATOMIC or B200_SCATTER_DETERMINISTIC */
@@ -155,7 +157,7 @@ typedef struct {
   const double  *interp_1d;   /* host, Q x P */
   const double  *grad_1d;     /* host, Q x P */
   int            elems_per_block; /* 0: tuned default */
-  int            staging;         /* 0: default, 1: registers, 2: shared memory */
+  int            staging;         /* 0: default, 1: registers, 2: shared memory, 3: persistent pipelined */
 } b200_op_desc;
 
 int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);
@@ -250,6 +252,11 @@ int b200_vec_dot_static(int prec, int64_t n, const void *x, const void *y, doubl
 
 int b200_cg_solve(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask, const double *b,
                   double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats);
+
+/* ---- Pipe throughput probe.  No counterpart in the reference: measures the fused multiply-add rate of the FP64
+ *      (prec B200_F64) or FP32 (B200_F32) pipe of the context's GPU with independent FMA chains on every SM, so that
+ *      compute-bound kernels report a fraction of a measured peak.  Blocks the host; *tflops = 2 * FMAs / s / 1e12. */
+int b200_fma_peak(b200_ctx ctx, int prec, double *tflops);
 
 #ifdef __cplusplus
 }

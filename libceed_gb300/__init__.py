@@ -5,6 +5,6 @@ libceed_b200.so (include/ceed-b200.h).  Build the library with `libceed_gb300.bu
 """
 from ._ffi import B200Error  # noqa: F401
 from .ceed import (  # noqa: F401
-    COPY_VALUES, EVAL_GRAD, EVAL_INTERP, EVAL_NONE, EVAL_WEIGHT, F32, F64, GAUSS, GAUSS_LOBATTO, MEM_DEVICE, MEM_HOST, NORM_1,
+    COPY_VALUES, EVAL_GRAD, EVAL_INTERP, EVAL_NONE, EVAL_WEIGHT, F32, F64, F64X, GAUSS, GAUSS_LOBATTO, MEM_DEVICE, MEM_HOST, NORM_1,
     NORM_2, NORM_MAX, NOTRANSPOSE, STRIDES_BACKEND, TRANSPOSE, USE_POINTER, Ceed,
 )

@@ -28,7 +28,7 @@ GAUSS, GAUSS_LOBATTO = basis1d.GAUSS, basis1d.GAUSS_LOBATTO
 REQUEST_IMMEDIATE = None
 STRIDES_BACKEND = "backend"
 SCATTER_ATOMIC, SCATTER_DETERMINISTIC = 0, 1
-F64, F32 = 0, 1
+F64, F32, F64X = 0, 1, 2  # F64X: float-float arithmetic on double vectors (fused operator only)
 
 # Gallery QFunctions on the hot path (include/ceed/jit-source/gallery/*.h), plus the kappa-weighted diffusion
 # this backend adds for the differentiable operator.  Fields: (name, size, eval mode).
@@ -94,6 +94,12 @@ class Ceed:
         n = ctypes.c_int64()
         call("b200_ctx_launch_count", self._ctx, ctypes.byref(n))
         return n.value
+
+    def fma_peak(self, prec=F64):
+        """Measured fused multiply-add rate of the FP64 or FP32 pipe (TFLOP/s), the compute roofline's denominator."""
+        t = ctypes.c_double()
+        call("b200_fma_peak", self._ctx, prec, ctypes.byref(t))
+        return t.value
 
     def gauss_quadrature(self, q):
         return basis1d.gauss_quadrature(q)
@@ -419,6 +425,8 @@ class Operator:
         self._fused = {}
         self.elems_per_block = 0
         self.staging = 0
+        # "native": the vectors' precision; "float-float": double vectors, FP32-pipe float-float arithmetic (F64X).
+        self.arithmetic = "native"
 
     def set_field(self, name, rstr, basis, vec):
         names = [f[0] for f in list(self.qf.inputs) + list(self.qf.outputs)]
@@ -455,6 +463,13 @@ class Operator:
     def fused(self, prec=F64):
         """The fused kernel object behind this operator (tile control, cost model)."""
         return self._fused_op(prec)
+
+    def _kernel_prec(self, prec):
+        if self.arithmetic == "native":
+            return prec
+        if self.arithmetic == "float-float" and prec == F64:
+            return F64X
+        raise B200Error("CeedOperatorApply", -2, f"arithmetic {self.arithmetic!r} needs double vectors")
 
     def _passive(self, name, prec):
         v = self.fields[name].vec
@@ -516,7 +531,7 @@ class Operator:
             return
         if isinstance(kind, str):
             return self._build(u, v, add)
-        op = self._fused_op(u.prec)
+        op = self._fused_op(self._kernel_prec(u.prec))
         qd = self._passive("qdata", u.prec)
         kap = self._passive("kappa", u.prec) if kind == QF_POISSON_KAPPA else None
         call("b200_op_apply", op.h, u.ptr(), v.ptr(), qd.ptr(), kap.ptr() if kap else _vp(0), 1 if add else 0)

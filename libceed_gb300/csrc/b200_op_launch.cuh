@@ -46,7 +46,7 @@ inline void make_eo(const double *M, int par, EOMat<T, J, K> &out) {
       out.O[j * Kh + k] = (T)(0.5 * (M[j * K + k] - M[j * K + K - 1 - k]));
     }
   for (int j = 0; j <= Jh; j++) out.C[j] = (T)((K % 2 && j < Jh) ? M[j * K + Kh] : 0.0);
-  for (int k = 0; k <= Kh; k++) out.R[k] = 0;
+  for (int k = 0; k <= Kh; k++) out.R[k] = (T)0.0;
   if (J % 2) {
     const double *row = M + Jh * K;
     for (int k = 0; k < Kh; k++) out.R[k] = (T)(par > 0 ? 0.5 * (row[k] + row[K - 1 - k]) : 0.5 * (row[k] - row[K - 1 - k]));
@@ -166,19 +166,27 @@ OpInstance op_instance_pipe() {
 
 template <typename T, int P, int QF>
 bool op_variant(int variant, OpInstance *out) {
-  switch (variant) {
-    case kVarReg: *out = op_instance<T, P, QF, kStageReg, false>(); return true;
-    case kVarSmem: *out = op_instance<T, P, QF, kStageSmem, false>(); return true;
-    case kVarRegEO: *out = op_instance<T, P, QF, kStageReg, true>(); return true;
-    case kVarSmemEO: *out = op_instance<T, P, QF, kStageSmem, true>(); return true;
-    case kVarPipeEO:
-      if constexpr (QFTraits<QF>::nc == 1) {
-        *out = op_instance_pipe<T, P, QF>();
-        return true;
-      } else {
-        return false;
-      }
-    default: return false;
+  if constexpr (__is_same(T, dfloat)) {
+    // Float-float: only the even-odd kernels (half the multiply-adds, which cost ~15 FP32 operations each).
+    if (variant == kVarRegEO) *out = op_instance<T, P, QF, kStageReg, true>();
+    else if (variant == kVarSmemEO) *out = op_instance<T, P, QF, kStageSmem, true>();
+    else return false;
+    return true;
+  } else {
+    switch (variant) {
+      case kVarReg: *out = op_instance<T, P, QF, kStageReg, false>(); return true;
+      case kVarSmem: *out = op_instance<T, P, QF, kStageSmem, false>(); return true;
+      case kVarRegEO: *out = op_instance<T, P, QF, kStageReg, true>(); return true;
+      case kVarSmemEO: *out = op_instance<T, P, QF, kStageSmem, true>(); return true;
+      case kVarPipeEO:
+        if constexpr (QFTraits<QF>::nc == 1) {
+          *out = op_instance_pipe<T, P, QF>();
+          return true;
+        } else {
+          return false;
+        }
+      default: return false;
+    }
   }
 }
 

@@ -25,6 +25,8 @@ bool op_table_f32_poisson(int, int, OpInstance *);
 bool op_table_f32_vecmass(int, int, OpInstance *);
 bool op_table_f32_vecpoisson(int, int, OpInstance *);
 bool op_table_f32_kappa(int, int, OpInstance *);
+bool op_table_f64x_mass(int, int, OpInstance *);
+bool op_table_f64x_poisson(int, int, OpInstance *);
 bool kgrad_table_f64(int, OpLauncher *);
 bool kgrad_table_f32(int, OpLauncher *);
 
@@ -46,9 +48,18 @@ bool op_lookup(int prec, int qf, int P, int variant, OpInstance *out) {
       case B200_QF_VECPOISSON: return op_table_f32_vecpoisson(P, variant, out);
       case B200_QF_POISSON_KAPPA: return op_table_f32_kappa(P, variant, out);
     }
+  } else if (prec == B200_F64X) {
+    switch (qf) {
+      case B200_QF_MASS: return op_table_f64x_mass(P, variant, out);
+      case B200_QF_POISSON: return op_table_f64x_poisson(P, variant, out);
+    }
   }
   return false;
 }
+
+// Element type of the vectors in HBM: B200_F64X stores double.
+static int storage_prec(int prec) { return prec == B200_F32 ? B200_F32 : B200_F64; }
+static size_t storage_bytes(int prec) { return prec == B200_F32 ? 4 : 8; }
 
 // True when M (J x K, row-major) satisfies M[J-1-j][K-1-k] = par * M[j][k] to rounding.
 static bool centro(const double *M, int J, int K, int par) {
@@ -142,16 +153,29 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
   return B200_SUCCESS;
 }
 
-// Default launch shape per precision and QFunction (measured on GB300; the autotuner refines it).
+// Default launch shape per precision and QFunction, from autotuner sweeps on GB300 (n^3 boxes of ~17M DoF, atomic
+// scatter).  Indexed by P_1d - 2; {staging, elements per block}.  The autotuner refines it per problem.
+struct TileDefault {
+  int stage, epb;
+};
+static const TileDefault kTileF64Grad[8]  = {{1, 28}, {1, 24}, {1, 5}, {1, 7}, {1, 5}, {1, 1}, {1, 2}, {2, 1}};
+static const TileDefault kTileF64Mass[8]  = {{1, 28}, {1, 8}, {1, 14}, {1, 8}, {1, 6}, {1, 2}, {1, 6}, {1, 2}};
+static const TileDefault kTileF32[8]      = {{1, 28}, {1, 6}, {1, 6}, {1, 6}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};
+static const TileDefault kTileF64XGrad[8] = {{1, 28}, {1, 10}, {1, 5}, {1, 7}, {1, 7}, {1, 1}, {2, 1}, {2, 1}};
+static const TileDefault kTileF64XMass[8] = {{1, 28}, {1, 8}, {1, 5}, {1, 5}, {1, 4}, {1, 4}, {1, 3}, {1, 2}};
+
 static void op_default_tile(b200_op op, int *epb, int *stage) {
-  const int Q = op->d.Q_1d;
-  if (*stage <= 0) {
-    if (op->d.num_comp > 1) *stage = kStageSmem;
-    else if (op->symmetric) *stage = kStagePipe;
-    else *stage = op->d.prec == B200_F64 ? kStageSmem : kStageReg;
+  const int Q = op->d.Q_1d, P = op->d.P_1d;
+  TileDefault t{kStageSmem, 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1};  // vector QFunctions
+  if (op->d.num_comp == 1 && P >= kOpPMin && P <= kOpPMax) {
+    const bool mass = op->d.qf == B200_QF_MASS;
+    if (op->d.prec == B200_F64) t = (mass ? kTileF64Mass : kTileF64Grad)[P - 2];
+    else if (op->d.prec == B200_F64X) t = (mass ? kTileF64XMass : kTileF64XGrad)[P - 2];
+    else t = kTileF32[P - 2];
   }
+  if (*stage <= 0) *stage = t.stage;
   if (*epb <= 0) {
-    *epb = 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1;
+    *epb = *stage == t.stage ? t.epb : (256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1);
     if (*stage == kStagePipe) *epb = 128 / (Q * Q) > 0 ? 128 / (Q * Q) : 1;
   }
 }
@@ -187,7 +211,9 @@ static int op_select(b200_op op, int epb, int stage) {
 
 extern "C" int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *out) {
   const b200_op_desc &d = *desc;
-  B200_CHECK(d.prec == B200_F64 || d.prec == B200_F32, B200_ERROR_UNSUPPORTED, "unknown precision %d", d.prec);
+  B200_CHECK(d.prec == B200_F64 || d.prec == B200_F32 || d.prec == B200_F64X, B200_ERROR_UNSUPPORTED, "unknown precision %d", d.prec);
+  B200_CHECK(d.prec != B200_F64X || d.qf == B200_QF_MASS || d.qf == B200_QF_POISSON, B200_ERROR_UNSUPPORTED,
+             "float-float kernels cover the scalar mass and Poisson QFunctions");
   B200_CHECK(d.Q_1d == d.P_1d + 1, B200_ERROR_UNSUPPORTED, "fused kernels are compiled for Q_1d = P_1d + 1 (got P=%d, Q=%d)", d.P_1d, d.Q_1d);
   B200_CHECK(d.P_1d >= kOpPMin && d.P_1d <= kOpPMax, B200_ERROR_UNSUPPORTED, "fused kernels cover P_1d in %d..%d (got %d)", kOpPMin, kOpPMax, d.P_1d);
   const int nc_expected = (d.qf == B200_QF_VECMASS || d.qf == B200_QF_VECPOISSON) ? 3 : 1;
@@ -210,10 +236,15 @@ extern "C" int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *o
     return B200_ERROR_BACKEND;
   }
   op->symmetric = centro(op->B.data(), Q, P, 1) && centro(op->Gc.data(), Q, Q, -1) && !getenv("CEED_B200_NO_EVEN_ODD");
+  if (d.prec == B200_F64X && !op->symmetric) {
+    delete op;
+    set_error("float-float kernels need a centro-symmetric basis (Lagrange on Gauss-Lobatto nodes, Gauss points)");
+    return B200_ERROR_UNSUPPORTED;
+  }
   int st = op_select(op, d.elems_per_block, d.staging);
   if (!st && d.scatter == B200_SCATTER_DETERMINISTIC && d.num_elem > 0) {
     st = b200_plan_create(ctx, d.num_elem, P * P * P, d.num_comp, d.comp_stride, d.l_size, nullptr, d.offsets, &op->plan);
-    const size_t esz = (d.prec == B200_F64 ? 8 : 4) * (size_t)d.num_elem * P * P * P * d.num_comp;
+    const size_t esz = storage_bytes(d.prec) * (size_t)d.num_elem * P * P * P * d.num_comp;
     if (!st) st = cuda_status(cudaMalloc(&op->e_work, esz), "cudaMalloc(e_work)", __FILE__, __LINE__);
   }
   if (st) {
@@ -239,7 +270,7 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   B200_CHECK(!op->jit, B200_ERROR_INCOMPATIBLE, "operator has a run-time compiled QFunction: use b200_op_apply_jit");
   B200_CHECK(u && v && qdata, B200_ERROR_INCOMPLETE, "b200_op_apply: u, v and qdata are required");
   B200_CHECK(d.qf != B200_QF_POISSON_KAPPA || kappa, B200_ERROR_INCOMPLETE, "kappa-weighted diffusion needs kappa");
-  const size_t tsz = d.prec == B200_F64 ? 8 : 4;
+  const size_t tsz = storage_bytes(d.prec);
   if (d.num_elem == 0) {
     if (!add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
     return B200_SUCCESS;
@@ -261,14 +292,14 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   if (!r.det && !add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
   int st = op->inst.launch(ctx, r);
   if (st) return st;
-  if (r.det) st = plan_scatter(op->plan, d.prec, op->e_work, v, add);
+  if (r.det) st = plan_scatter(op->plan, storage_prec(d.prec), op->e_work, v, add);
   return st;
 }
 
 extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qdata, void *g) {
   b200_ctx            ctx = op->ctx;
   const b200_op_desc &d   = op->d;
-  B200_CHECK(d.qf == B200_QF_POISSON_KAPPA, B200_ERROR_INCOMPATIBLE, "kappa gradient needs the kappa-weighted diffusion operator");
+  B200_CHECK(d.qf == B200_QF_POISSON_KAPPA && d.prec != B200_F64X, B200_ERROR_INCOMPATIBLE, "kappa gradient needs the kappa-weighted diffusion operator");
   if (d.num_elem == 0) return B200_SUCCESS;
   OpLauncher launch;
   B200_CHECK(kgrad_lookup(d.prec, d.P_1d, &launch), B200_ERROR_UNSUPPORTED, "no kappa-gradient kernel for P=%d", d.P_1d);
@@ -277,7 +308,7 @@ extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, cons
   r.comp_stride = d.comp_stride;
   const int Q   = d.Q_1d;
   r.epb         = 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1;
-  while (r.epb > 1 && (size_t)(d.prec == B200_F64 ? 8 : 4) * r.epb * tile_team_stride(Q, 0) > 96 * 1024) r.epb--;
+  while (r.epb > 1 && (size_t)storage_bytes(d.prec) * r.epb * tile_team_stride(Q, 0) > 96 * 1024) r.epb--;
   r.offsets = d.offsets;
   r.u       = u;
   r.w       = w;
@@ -291,7 +322,7 @@ extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, cons
 extern "C" int b200_op_cost(b200_op op, double *bytes, double *flops) {
   const b200_op_desc &d  = op->d;
   const double        P  = d.P_1d, Q = d.Q_1d, ne = (double)d.num_elem, nc = d.num_comp;
-  const double        ts = d.prec == B200_F64 ? 8.0 : 4.0;
+  const double        ts = (double)storage_bytes(d.prec);
   const bool          grad = d.qf == B200_QF_POISSON || d.qf == B200_QF_VECPOISSON || d.qf == B200_QF_POISSON_KAPPA;
   const double        nqd  = grad ? 6.0 : 1.0;
   // Algorithmic bytes: read u, write v, read offsets, read qdata (and kappa) once each.
@@ -332,7 +363,7 @@ extern "C" int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_b
   int        variant;
   *max_elems_per_block = 0;
   if (op_variant_of(op, staging, &variant)) return B200_SUCCESS;  // staging not available for this operator: no tiles
-  B200_CHECK(op_lookup(op->d.prec, op->d.qf, op->d.P_1d, variant, &inst), B200_ERROR_UNSUPPORTED, "no kernel for staging %d", staging);
+  if (!op_lookup(op->d.prec, op->d.qf, op->d.P_1d, variant, &inst)) return B200_SUCCESS;  // no instance for this staging
   int m = inst.max_threads / Q2;
   while (m > 1 && inst.smem(m) > 200 * 1024) m--;
   *max_elems_per_block = m < 1 ? 0 : m;
@@ -360,7 +391,7 @@ static int op_common_init(b200_ctx ctx, const b200_op_desc &d, b200_op op) {
   if (d.scatter == B200_SCATTER_DETERMINISTIC && d.num_elem > 0) {
     int st = b200_plan_create(ctx, d.num_elem, P * P * P, d.num_comp, d.comp_stride, d.l_size, nullptr, d.offsets, &op->plan);
     if (st) return st;
-    const size_t esz = (d.prec == B200_F64 ? 8 : 4) * (size_t)d.num_elem * P * P * P * d.num_comp;
+    const size_t esz = storage_bytes(d.prec) * (size_t)d.num_elem * P * P * P * d.num_comp;
     B200_CUDA(cudaMalloc(&op->e_work, esz));
   }
   return B200_SUCCESS;
@@ -424,7 +455,7 @@ extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void 
   const b200_op_desc &d   = op->d;
   B200_CHECK(op->jit, B200_ERROR_INCOMPATIBLE, "operator has a compiled pointwise kernel: use b200_op_apply");
   B200_CHECK(u && v, B200_ERROR_INCOMPLETE, "b200_op_apply_jit: u and v are required");
-  const size_t tsz = d.prec == B200_F64 ? 8 : 4;
+  const size_t tsz = storage_bytes(d.prec);
   if (!add && d.scatter == B200_SCATTER_ATOMIC) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
   if (d.num_elem == 0) return B200_SUCCESS;
   // Kernel arguments: OpArgs<T>, JitFields<T>, OpMats<T, P, Q> (bytes prepared at create).
@@ -450,7 +481,7 @@ extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void 
   const int64_t grid = ceil_div(d.num_elem, op->epb);
   B200_CUDA(cudaLaunchKernel((const void *)op->jit_kernel, dim3((unsigned)grid), dim3(op->epb * Q * Q), params, smem, ctx->stream));
   B200_LAUNCHED(ctx, "op_apply_jit");
-  if (d.scatter == B200_SCATTER_DETERMINISTIC) return plan_scatter(op->plan, d.prec, op->e_work, v, add);
+  if (d.scatter == B200_SCATTER_DETERMINISTIC) return plan_scatter(op->plan, storage_prec(d.prec), op->e_work, v, add);
   return B200_SUCCESS;
 }
 

@@ -6,14 +6,16 @@
 // as in include/ceed/jit-source/gallery/ceed-poisson3dbuild.h and ceed-poisson3dapply.h.
 #pragma once
 
+#include "b200_dfloat.cuh"
+
 namespace b200 {
 
-// vg_j = sum_i ug_i D_ij  (Poisson3DApply), evaluated left to right like the gallery source.
+// vg_j = sum_i ug_i D_ij  (Poisson3DApply), accumulated left to right like the gallery source.
 template <typename T>
 __device__ __forceinline__ void poisson_point(const T D[6], T gx, T gy, T gz, T vg[3]) {
-  vg[0] = gx * D[0] + gy * D[5] + gz * D[4];
-  vg[1] = gx * D[5] + gy * D[1] + gz * D[3];
-  vg[2] = gx * D[4] + gy * D[3] + gz * D[2];
+  vg[0] = mad(gz, D[4], mad(gy, D[5], gx * D[0]));
+  vg[1] = mad(gz, D[3], mad(gy, D[1], gx * D[5]));
+  vg[2] = mad(gz, D[2], mad(gy, D[3], gx * D[4]));
 }
 
 // qdata = w * det(J)  (Mass3DBuild); J[d][c] = d x_c / d xi_d.

@@ -2,6 +2,8 @@
 
     python -m libceed_gb300.profile_case --degree 4 --prec f64 --n 32 --reps 3 [--det] [--epb E --staging S]
 
+--prec f64x runs the float-float kernels on the same double vectors.
+
 Builds the Poisson operator of an n^3 box (qdata of n=32 at degree 4: 340 MB in FP64, larger than L2), applies it
 `reps` times and prints the mean device time.  The fused kernel is `k_op_apply`.
 """
@@ -17,7 +19,7 @@ from libceed_gb300.smoke_case import build_poisson
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--degree", type=int, default=4)
-    ap.add_argument("--prec", choices=["f64", "f32"], default="f64")
+    ap.add_argument("--prec", choices=["f64", "f32", "f64x"], default="f64")
     ap.add_argument("--n", type=int, default=32)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--det", action="store_true")
@@ -26,13 +28,15 @@ def main():
     ap.add_argument("--epb", type=int, default=0)
     ap.add_argument("--staging", type=int, default=0)
     a = ap.parse_args()
-    dt = torch.float64 if a.prec == "f64" else torch.float32
+    dt = torch.float32 if a.prec == "f32" else torch.float64
     ceed = lc.Ceed("/gpu/cuda/b200", deterministic=a.det)
     box = mesh.Box(a.n, a.degree, ncomp=a.ncomp, noise=0.05, seed=1)
     qf = ("Vector3MassApply" if a.ncomp == 3 else "MassApply") if a.mass else None
     objs = build_poisson(ceed, box, dtype=dt, qf_name=qf)
     op = objs["op"]
     op.elems_per_block, op.staging = a.epb, a.staging
+    if a.prec == "f64x":
+        op.arithmetic = "float-float"
     u = ceed.Vector(box.l_size, dt)
     u.set_array(box.u())
     v = ceed.Vector(box.l_size, dt)
@@ -45,7 +49,7 @@ def main():
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / a.reps
-    fused = op.fused(lc.F64 if dt == torch.float64 else lc.F32)
+    fused = op.fused({"f64": lc.F64, "f32": lc.F32, "f64x": lc.F64X}[a.prec])
     b, f = fused.cost()
     print(f"degree {a.degree} {a.prec} n={a.n} dof={box.l_size} tile={fused.tile()} {ms:.4f} ms/apply "
           f"{box.l_size / ms / 1e6:.3f} GDoF/s {b / ms / 1e6:.1f} GB/s(alg) {f / ms / 1e9:.3f} TFLOP/s alg_bytes={b:.0f}")

@@ -13,7 +13,7 @@ import json
 import os
 
 from ._ffi import call
-from .ceed import F32, F64, QF_POISSON_KAPPA
+from .ceed import F32, F64, F64X, QF_POISSON_KAPPA
 
 STAGE_NAMES = {1: "registers", 2: "shared", 3: "pipelined"}
 STAGE_CODES = {v: k for k, v in STAGE_NAMES.items()}
@@ -26,7 +26,8 @@ def cache_path():
 def _key(op, prec):
     f = op._active_input()
     b, r = f.basis, f.rstr
-    return f"dim{b.dim}_P{b.P1d}_Q{b.Q1d}_nc{r.ncomp}_{'f64' if prec == F64 else 'f32'}_{op.qf.name}_{'det' if op.ceed.deterministic else 'atomic'}"
+    pname = {F64: "f64", F32: "f32", F64X: "f64x"}[prec]
+    return f"dim{b.dim}_P{b.P1d}_Q{b.Q1d}_nc{r.ncomp}_{pname}_{op.qf.name}_{'det' if op.ceed.deterministic else 'atomic'}"
 
 
 def load_cache():
@@ -48,12 +49,12 @@ def save_cache(cache):
 
 def autotune(op, u, v, reps=5, candidates=None, use_cache=True, log=None):
     """Sweep the launch shape of `op` on vectors u, v; set and return the best {epb, staging, ms, key, sweep}."""
-    prec = u.prec
+    prec = op._kernel_prec(u.prec)
     fused = op.fused(prec)
     key = _key(op, prec)
     cache = load_cache() if use_cache else {}
-    qd = op._passive("qdata", prec)
-    kap = op._passive("kappa", prec) if op.qf.kind == QF_POISSON_KAPPA else None
+    qd = op._passive("qdata", u.prec)
+    kap = op._passive("kappa", u.prec) if op.qf.kind == QF_POISSON_KAPPA else None
     sweep = []
     for stage in (1, 2, 3):
         m = ctypes.c_int()
