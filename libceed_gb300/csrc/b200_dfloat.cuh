@@ -11,14 +11,59 @@
 
 namespace b200 {
 
+__host__ __device__ inline unsigned df_bits_f(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  unsigned u;
+  __builtin_memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+__host__ __device__ inline float df_f_bits(unsigned u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f;
+  __builtin_memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+
+// Split a double into a float-float pair with integer and FP32 operations only (no FP64 pipe: on this GPU the
+// double<->float conversions issue on the slow FP64 pipe and would bound the float-float kernels).  hi keeps the
+// leading 24 significant bits of x (truncated), lo = x - hi rounded to float: |lo| < ulp(hi) and hi + lo = x to a
+// relative 2^-47.  Values outside [2^-74, 2^128) in magnitude take the conversion route (zero directly).
+__host__ __device__ inline void df_split(double x, float &hi, float &lo) {
+  unsigned long long b;
+#ifdef __CUDA_ARCH__
+  b = (unsigned long long)__double_as_longlong(x);
+#else
+  __builtin_memcpy(&b, &x, 8);
+#endif
+  const unsigned h32 = (unsigned)(b >> 32), l32 = (unsigned)b;
+  const int      E   = (int)((h32 >> 20) & 0x7FFu);  // biased exponent
+  if (E >= 949 && E <= 1150) {
+    const unsigned sign = h32 & 0x80000000u;
+    hi                  = df_f_bits(sign | ((unsigned)(E - 896) << 23) | ((h32 & 0xFFFFFu) << 3) | (l32 >> 29));
+    const unsigned r    = l32 & 0x1FFFFFFFu;  // the 29 low significand bits, weight 2^(E - 1075)
+    const float    rh   = df_f_bits(0x4B000000u | (r >> 6)) - 8388608.0f;  // exact: r >> 6 < 2^23
+    const float    rl   = df_f_bits(0x4B000000u | (r & 63u)) - 8388608.0f;
+    const float    rv   = rh * 64.0f + rl;                                  // r, rounded once to 24 bits
+    lo                  = df_f_bits(df_bits_f(rv * df_f_bits((unsigned)(E - 948) << 23)) | sign);
+  } else if ((b << 1) == 0) {
+    hi = lo = 0.0f;
+  } else {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+  }
+}
+
 struct dfloat {
   float hi, lo;
   __host__ __device__ dfloat() : hi(0.f), lo(0.f) {}
   __host__ __device__ explicit dfloat(int x) : hi((float)x), lo(0.f) {}
-  __host__ __device__ explicit dfloat(double x) {
-    hi = (float)x;
-    lo = (float)(x - (double)hi);
-  }
+  __host__ __device__ explicit dfloat(double x) { df_split(x, hi, lo); }
   __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
 };
 

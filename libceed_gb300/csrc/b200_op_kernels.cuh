@@ -25,6 +25,9 @@
 //   k_op_apply_pipe            persistent blocks looping over element batches with a two-deep software pipeline:
 //                              while batch i is computed, batch i+1's qdata streams into a second shared-memory buffer
 //                              (cp.async) and its u values and batch i+2's offsets are loaded into registers.
+//   k_op_apply_3d              "point" mapping: a team of Q^3 threads per element, one thread per output point of
+//                              each stage (Q*P*P, Q*Q*P, Q^3, ... threads active), the 1D matrices in shared memory
+//                              and the thread's own qdata in registers (one coalesced load per component).
 #pragma once
 
 #ifndef __CUDACC_RTC__
@@ -36,7 +39,7 @@
 
 namespace b200 {
 
-enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3 };
+enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4 };  // kStage3D: point mapping (k_op_apply_3d)
 
 // Shared-memory layout of an element tile: point (x, y, z) at x + Q*y + tile_plane(Q)*z, three tiles per team
 // (tile_buf each), and a team stride that is fixed modulo 32 words.  The plane padding and the team stride residue
@@ -502,6 +505,124 @@ __global__ void k_op_apply_pipe(const OpArgs<typename Store<T>::type> args, cons
     buf ^= 1;
   }
   cp_async_wait<0>();
+}
+
+// Shared memory of the point-mapped kernel: the 1D matrices (B, then G_c), padded to 32 elements, then one team of
+// three tiles per element.
+template <typename T, int P, int Q>
+struct Op3DShape {
+  static constexpr int mats = (Q * P + Q * Q + 31) / 32 * 32;
+  static constexpr int team = tile_team_stride(Q, 0);
+};
+
+// Point ("3D") thread mapping.  Team thread t is point (x, y, z) = (t % Q, t / Q % Q, t / Q^2) of the element's Q^3
+// grid; each stage of the sum factorization lets the first (outputs of the stage) threads compute one output each as
+// a length-P or length-Q dot product over a shared tile.  Same stages and result as k_op_apply (general, not even-odd
+// contractions); every thread reads its own point's qdata once.
+template <typename T, int P, int Q, int QF>
+__global__ void k_op_apply_3d(const OpArgs<T> args, const OpMats<T, P, Q> M) {
+  using TR         = QFTraits<QF>;
+  using SH         = Op3DShape<T, P, Q>;
+  constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P2 = P * P, P3 = P * P * P, NC = TR::nc, NQD = TR::nqd;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T            *sB = reinterpret_cast<T *>(smem_raw), *sG = sB + Q * P;
+  const int     t = threadIdx.x % Q3, slot = threadIdx.x / Q3;
+  const int64_t e      = (int64_t)blockIdx.x * args.epb + slot;
+  const bool    active = e < args.num_elem;
+  const int64_t ne     = args.num_elem;
+  T            *s0 = sB + SH::mats + slot * SH::team, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q);
+  for (int i = threadIdx.x; i < Q * P; i += blockDim.x) sB[i] = M.B[i];
+  for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) sG[i] = M.G[i];
+  const int x = t % Q, y = (t / Q) % Q, z = t / Q2;
+  T         D[NQD];
+  {
+    T kap = T(1);
+    if constexpr (TR::kappa) kap = active ? args.kappa[e * Q3 + t] : T(0);
+#pragma unroll
+    for (int k = 0; k < NQD; k++) D[k] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + t] * kap : T(0);
+  }
+  const int32_t my_off = (active && t < P3) ? args.offsets[e * P3 + t] : 0;
+
+#pragma unroll 1
+  for (int c = 0; c < NC; c++) {
+    __syncthreads();  // matrices in place (c = 0), tiles free again (c > 0)
+    if (t < P3) s0[B200_IDX(t % P, (t / P) % P, t / P2)] = active ? args.u[(int64_t)my_off + c * args.comp_stride] : T(0);
+    __syncthreads();
+    if (t < Q * P2) {  // X interpolation: (i < Q, j < P, k < P)
+      const int i = t % Q, j = (t / Q) % P, k = t / (Q * P);
+      T         s = T(0);
+#pragma unroll
+      for (int m = 0; m < P; m++) s = mad(sB[i * P + m], s0[B200_IDX(m, j, k)], s);
+      s1[B200_IDX(i, j, k)] = s;
+    }
+    __syncthreads();
+    if (t < Q2 * P) {  // Y interpolation: (i < Q, j < Q, k < P)
+      const int i = t % Q, j = (t / Q) % Q, k = t / Q2;
+      T         s = T(0);
+#pragma unroll
+      for (int m = 0; m < P; m++) s = mad(sB[j * P + m], s1[B200_IDX(i, m, k)], s);
+      s0[B200_IDX(i, j, k)] = s;
+    }
+    __syncthreads();
+    T U = T(0);  // Z interpolation: every point
+#pragma unroll
+    for (int m = 0; m < P; m++) U = mad(sB[z * P + m], s0[B200_IDX(x, y, m)], U);
+    T w;
+    if constexpr (TR::grad) {
+      s1[B200_IDX(x, y, z)] = U;
+      __syncthreads();
+      T g0 = T(0), g1 = T(0), g2 = T(0);
+#pragma unroll
+      for (int m = 0; m < Q; m++) {
+        g0 = mad(sG[x * Q + m], s1[B200_IDX(m, y, z)], g0);
+        g1 = mad(sG[y * Q + m], s1[B200_IDX(x, m, z)], g1);
+        g2 = mad(sG[z * Q + m], s1[B200_IDX(x, y, m)], g2);
+      }
+      T vg[3];
+      poisson_point(D, g0, g1, g2, vg);
+      __syncthreads();
+      s0[B200_IDX(x, y, z)] = vg[0];
+      s1[B200_IDX(x, y, z)] = vg[1];
+      s2[B200_IDX(x, y, z)] = vg[2];
+      __syncthreads();
+      w = T(0);
+#pragma unroll
+      for (int m = 0; m < Q; m++) {
+        w = mad(sG[m * Q + x], s0[B200_IDX(m, y, z)], w);
+        w = mad(sG[m * Q + y], s1[B200_IDX(x, m, z)], w);
+        w = mad(sG[m * Q + z], s2[B200_IDX(x, y, m)], w);
+      }
+    } else {
+      w = U * D[0];
+    }
+    __syncthreads();
+    s0[B200_IDX(x, y, z)] = w;
+    __syncthreads();
+    if (t < Q2 * P) {  // Z interpolation transposed: (i < Q, j < Q, k < P)
+      const int i = t % Q, j = (t / Q) % Q, k = t / Q2;
+      T         s = T(0);
+#pragma unroll
+      for (int m = 0; m < Q; m++) s = mad(sB[m * P + k], s0[B200_IDX(i, j, m)], s);
+      s1[B200_IDX(i, j, k)] = s;
+    }
+    __syncthreads();
+    if (t < Q * P2) {  // Y interpolation transposed: (i < Q, j < P, k < P)
+      const int i = t % Q, j = (t / Q) % P, k = t / (Q * P);
+      T         s = T(0);
+#pragma unroll
+      for (int m = 0; m < Q; m++) s = mad(sB[m * P + j], s1[B200_IDX(i, m, k)], s);
+      s0[B200_IDX(i, j, k)] = s;
+    }
+    __syncthreads();
+    if (t < P3 && active) {  // X interpolation transposed and scatter: node (i, j, k) = t
+      const int i = t % P, j = (t / P) % P, k = t / P2;
+      T         s = T(0);
+#pragma unroll
+      for (int m = 0; m < Q; m++) s = mad(sB[m * P + i], s0[B200_IDX(m, j, k)], s);
+      if (args.det) args.e_out[((int64_t)c * ne + e) * P3 + t] = s;
+      else atomicAdd(&args.v[(int64_t)my_off + c * args.comp_stride], s);
+    }
+  }
 }
 
 // Gradient of the kappa-weighted diffusion with respect to kappa: g[e][q] = grad(w)_q . D_q grad(u)_q, both gradients

@@ -11,7 +11,7 @@ namespace b200 {
 constexpr int kOpPMin = 2, kOpPMax = 9;  // compiled range of P_1d (Q_1d = P_1d + 1)
 
 // Kernel variants: qdata staging x contraction form.
-enum { kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kNumVariants = 5 };
+enum { kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kVar3D = 5, kNumVariants = 6 };
 
 // Untyped launch request; pointers are reinterpreted in the instance's precision.
 struct OpLaunch {
@@ -126,6 +126,37 @@ int op_launch_pipe(b200_ctx ctx, const OpLaunch &r) {
   return B200_SUCCESS;
 }
 
+template <typename T, int P, int QF>
+size_t op_smem_3d(int epb) {
+  using SH = Op3DShape<T, P, P + 1>;
+  return sizeof(T) * ((size_t)SH::mats + (size_t)epb * SH::team);
+}
+
+template <typename T, int P, int QF>
+int op_launch_3d(b200_ctx ctx, const OpLaunch &r) {
+  constexpr int Q    = P + 1;
+  auto          kern = k_op_apply_3d<T, P, Q, QF>;
+  const size_t  smem = op_smem_3d<T, P, QF>(r.epb);
+  if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = ceil_div(r.num_elem, r.epb);
+  kern<<<(unsigned)grid, r.epb * Q * Q * Q, smem, ctx->stream>>>(make_args<T>(r), make_mats<T, P, Q>(r.B, r.G));
+  B200_LAUNCHED(ctx, "op_apply_3d");
+  return B200_SUCCESS;
+}
+
+template <typename T, int P, int QF>
+int op_occupancy_3d(int epb) {
+  return blocks_per_sm(k_op_apply_3d<T, P, P + 1, QF>, epb * (P + 1) * (P + 1) * (P + 1), op_smem_3d<T, P, QF>(epb));
+}
+
+template <typename T, int P, int QF>
+OpInstance op_instance_3d() {
+  OpInstance         inst{op_launch_3d<T, P, QF>, op_smem_3d<T, P, QF>, op_occupancy_3d<T, P, QF>, 1024, false};
+  cudaFuncAttributes attr;
+  if (cudaFuncGetAttributes(&attr, k_op_apply_3d<T, P, P + 1, QF>) == cudaSuccess) inst.max_threads = attr.maxThreadsPerBlock;
+  return inst;
+}
+
 template <typename T, int P>
 int kgrad_launch(b200_ctx ctx, const OpLaunch &r) {
   constexpr int Q    = P + 1;
@@ -185,6 +216,7 @@ bool op_variant(int variant, OpInstance *out) {
         } else {
           return false;
         }
+      case kVar3D: *out = op_instance_3d<T, P, QF>(); return true;
       default: return false;
     }
   }

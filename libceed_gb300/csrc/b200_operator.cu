@@ -147,6 +147,8 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
     B200_CHECK(eo && op->d.num_comp == 1, B200_ERROR_UNSUPPORTED,
                "the pipelined kernel needs one component and a centro-symmetric basis (Lagrange on Gauss-Lobatto nodes, Gauss points)");
     *variant = kVarPipeEO;
+  } else if (stage == kStage3D) {
+    *variant = kVar3D;
   } else {
     B200_CHECK(false, B200_ERROR_UNSUPPORTED, "unknown qdata staging %d", stage);
   }
@@ -177,12 +179,16 @@ static void op_default_tile(b200_op op, int *epb, int *stage) {
   if (*epb <= 0) {
     *epb = *stage == t.stage ? t.epb : (256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1);
     if (*stage == kStagePipe) *epb = 128 / (Q * Q) > 0 ? 128 / (Q * Q) : 1;
+    if (*stage == kStage3D) *epb = 512 / (Q * Q * Q) > 0 ? 512 / (Q * Q * Q) : 1;
   }
 }
 
+// Threads per element of a staging choice: Q^2 (line mapping) or Q^3 (point mapping).
+static int team_threads(const b200_op_desc &d, int stage) { return stage == kStage3D ? d.Q_1d * d.Q_1d * d.Q_1d : d.Q_1d * d.Q_1d; }
+
 static int op_select(b200_op op, int epb, int stage) {
-  const int Q = op->d.Q_1d, Q2 = Q * Q;
   op_default_tile(op, &epb, &stage);
+  const int Q2 = team_threads(op->d, stage);
   int variant;
   int st = op_variant_of(op, stage, &variant);
   if (st) return st;
@@ -259,7 +265,7 @@ extern "C" int b200_op_set_tile(b200_op op, int elems_per_block, int staging) { 
 
 extern "C" int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_per_block, int *staging) {
   if (elems_per_block) *elems_per_block = op->epb;
-  if (threads_per_block) *threads_per_block = op->epb * op->d.Q_1d * op->d.Q_1d;
+  if (threads_per_block) *threads_per_block = op->epb * team_threads(op->d, op->stage);
   if (staging) *staging = op->stage;
   return B200_SUCCESS;
 }
@@ -359,7 +365,7 @@ extern "C" int b200_op_time(b200_op op, const void *u, void *v, const void *qdat
 
 extern "C" int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block) {
   OpInstance inst;
-  const int  Q2 = op->d.Q_1d * op->d.Q_1d;
+  const int  Q2 = team_threads(op->d, staging);
   int        variant;
   *max_elems_per_block = 0;
   if (op_variant_of(op, staging, &variant)) return B200_SUCCESS;  // staging not available for this operator: no tiles
