@@ -139,8 +139,9 @@ def ncu_traffic(key):
     """DRAM bytes per launch of the fused kernel from the committed ncu summary (profiles/traffic.json)."""
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f).get(key)
-    except (OSError, ValueError):
+            entry = json.load(f).get(key)
+        return entry["bytes_per_launch"] if entry else None
+    except (OSError, ValueError, KeyError):
         return None
 
 

@@ -360,15 +360,22 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   T *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q), *sq = s2 + tile_buf(Q);
 
   // ---- qdata staging ------------------------------------------------------------------------------------------------
+  // Register staging keeps the loaded storage values (S) and converts at first use, so that the loads stay in flight
+  // through the interpolation stages also when T is not the storage type.
+  using S          = typename Store<T>::type;
   constexpr int RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1;
-  T             rq[RQ][RZ];
+  S             rq[RQ][RZ];
   if constexpr (STAGE == kStageReg) {
+    static_assert(!TR::kappa || __is_same(S, T), "kappa-weighted kernels compute in the storage type");
 #pragma unroll
     for (int z = 0; z < Q; z++) {
-      T kap = T(1);
-      if constexpr (TR::kappa) kap = active ? T(args.kappa[e * Q3 + B200_QLIN(a, b, z)]) : T(0);
+      S kap = S(1);
+      if constexpr (TR::kappa) kap = active ? args.kappa[e * Q3 + B200_QLIN(a, b, z)] : S(0);
 #pragma unroll
-      for (int k = 0; k < NQD; k++) rq[k][z] = active ? T(args.qdata[((int64_t)k * ne + e) * Q3 + B200_QLIN(a, b, z)]) * kap : T(0);
+      for (int k = 0; k < NQD; k++) {
+        rq[k][z] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_QLIN(a, b, z)] : S(0);
+        if constexpr (TR::kappa) rq[k][z] *= kap;
+      }
     }
   } else {
     for (int i = tid; i < NQD * Q3; i += Q2) {
@@ -379,7 +386,7 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
       for (int q = tid; q < Q3; q += Q2) sq[NQD * Q3 + q] = active ? T(args.kappa[e * Q3 + q]) : T(0);
   }
   auto qd = [&](int k, int z) -> T {
-    if constexpr (STAGE == kStageReg) return rq[k][z];
+    if constexpr (STAGE == kStageReg) return T(rq[k][z]);
     else {
       const int q = B200_QLIN(a, b, z);
       if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];

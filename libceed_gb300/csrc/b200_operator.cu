@@ -160,8 +160,8 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
 struct TileDefault {
   int stage, epb;
 };
-static const TileDefault kTileF64Grad[8]  = {{1, 28}, {1, 24}, {1, 5}, {1, 7}, {1, 5}, {1, 1}, {1, 2}, {2, 1}};
-static const TileDefault kTileF64Mass[8]  = {{1, 28}, {1, 8}, {1, 14}, {1, 8}, {1, 6}, {1, 2}, {1, 6}, {1, 2}};
+static const TileDefault kTileF64Grad[8]  = {{1, 14}, {4, 5}, {1, 5}, {4, 1}, {1, 5}, {1, 1}, {1, 2}, {2, 1}};
+static const TileDefault kTileF64Mass[8]  = {{1, 28}, {1, 8}, {1, 14}, {4, 1}, {1, 6}, {1, 2}, {1, 6}, {1, 2}};
 static const TileDefault kTileF32[8]      = {{1, 28}, {1, 6}, {1, 6}, {1, 6}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};
 static const TileDefault kTileF64XGrad[8] = {{1, 28}, {1, 10}, {1, 5}, {1, 7}, {1, 7}, {1, 1}, {2, 1}, {2, 1}};
 static const TileDefault kTileF64XMass[8] = {{1, 28}, {1, 8}, {1, 5}, {1, 5}, {1, 4}, {1, 4}, {1, 3}, {1, 2}};
