@@ -38,17 +38,24 @@ typedef struct {
   b200_basis basis;
 } CeedBasis_B200;
 
+#define CEED_B200_QF_JIT (-3)  // user QFunction from a source file, compiled at run time with NVRTC
+
 typedef struct {
-  int qf_kind;  // B200_QF_*, -1 for the geometric-factor builds, -2 unsupported
+  int qf_kind;  // B200_QF_*, -1 for the geometric-factor builds, CEED_B200_QF_JIT, -2 unsupported
   int build_poisson;
 } CeedQFunction_B200;
 
 typedef struct {
   b200_op     op;
-  int         kind;  // 0 not analysed, 1 fused apply, 2 geometric-factor build, -1 unsupported
+  int         kind;  // 0 not analysed, 1 fused apply, 2 geometric-factor build, 3 run-time compiled QFunction, -1 unsupported
   CeedVector  qdata, kappa;
   CeedElemRestriction rstr_u, rstr_x;
   CeedBasis   basis_x;
+  // kind 3: passive inputs in QFunction order (without the active one) and the device copy of the context
+  CeedInt     num_passive;
+  CeedVector  passive[8];
+  void       *d_ctx;
+  size_t      ctx_size;
 } CeedOperator_B200;
 
 CEED_INTERN int CeedVectorCreate_B200(CeedSize n, CeedVector vec);

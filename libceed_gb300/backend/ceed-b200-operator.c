@@ -5,7 +5,11 @@
 //   apply:  active input/output through one offset restriction and one 3D tensor H1 basis with Q = P + 1, a gallery
 //           pointwise kernel (MassApply, Poisson3DApply, Vector3MassApply, Vector3Poisson3DApply), and qdata as a
 //           passive CEED_EVAL_NONE field through a strided restriction with backend strides -> b200_op_apply;
-//   setup:  Mass3DBuild / Poisson3DBuild with a trilinear coordinate field -> b200_qdata_build.
+//   setup:  Mass3DBuild / Poisson3DBuild with a trilinear coordinate field -> b200_qdata_build;
+//   user:   a QFunction from a source file with one active input (CEED_EVAL_INTERP or GRAD) and one active output
+//           through one offset restriction and 3D tensor basis with Q = P + 1, passive inputs CEED_EVAL_NONE through
+//           backend-strided restrictions -> NVRTC-compiled fused kernel (b200_op_create_jit / b200_op_apply_jit), as
+//           the reference's cuda-gen backend compiles its generated kernel (backends/cuda/ceed-cuda-compile.cpp).
 // Anything else returns CEED_ERROR_UNSUPPORTED: this backend has no CPU fallback and no delegate.
 #include <string.h>
 
@@ -15,6 +19,140 @@ static int FieldParts(CeedOperatorField f, CeedElemRestriction *r, CeedBasis *b,
   CeedCallBackend(CeedOperatorFieldGetElemRestriction(f, r));
   CeedCallBackend(CeedOperatorFieldGetBasis(f, b));
   CeedCallBackend(CeedOperatorFieldGetVector(f, v));
+  return CEED_ERROR_SUCCESS;
+}
+
+// Fill the parts of the fused-operator descriptor that come from the active restriction and basis.
+static int ActiveDesc(Ceed ceed, CeedElemRestriction ru, CeedBasis bu, b200_op_desc *d) {
+  CeedInt                   dim, P, Q, nc, ne, comp_stride;
+  CeedSize                  l_size;
+  bool                      is_tensor, det;
+  const CeedScalar         *interp, *grad;
+  CeedRestrictionType       type;
+  CeedElemRestriction_B200 *r_impl;
+
+  CeedCallBackend(CeedElemRestrictionGetType(ru, &type));
+  CeedCallBackend(CeedBasisIsTensor(bu, &is_tensor));
+  CeedCallBackend(CeedBasisGetDimension(bu, &dim));
+  CeedCallBackend(CeedBasisGetNumNodes1D(bu, &P));
+  CeedCallBackend(CeedBasisGetNumQuadraturePoints1D(bu, &Q));
+  CeedCheck(type == CEED_RESTRICTION_STANDARD && is_tensor && dim == 3 && Q == P + 1, ceed, CEED_ERROR_UNSUPPORTED,
+            "fused apply needs an offset restriction and a 3D tensor basis with Q = P + 1");
+  CeedCallBackend(CeedElemRestrictionGetNumComponents(ru, &nc));
+  CeedCallBackend(CeedElemRestrictionGetNumElements(ru, &ne));
+  CeedCallBackend(CeedElemRestrictionGetCompStride(ru, &comp_stride));
+  CeedCallBackend(CeedElemRestrictionGetLVectorSize(ru, &l_size));
+  CeedCallBackend(CeedBasisGetInterp1D(bu, &interp));
+  CeedCallBackend(CeedBasisGetGrad1D(bu, &grad));
+  CeedCallBackend(CeedIsDeterministic(ceed, &det));
+  CeedCallBackend(CeedElemRestrictionGetData(ru, &r_impl));
+  memset(d, 0, sizeof *d);
+  d->prec        = B200_F64;
+  d->P_1d        = P;
+  d->Q_1d        = Q;
+  d->num_comp    = nc;
+  d->scatter     = det ? B200_SCATTER_DETERMINISTIC : B200_SCATTER_ATOMIC;
+  d->num_elem    = ne;
+  d->l_size      = l_size;
+  d->comp_stride = comp_stride;
+  d->offsets     = r_impl->d_offsets;
+  d->interp_1d   = interp;
+  d->grad_1d     = grad;
+  return CEED_ERROR_SUCCESS;
+}
+
+// User QFunction: match the field pattern, compile with NVRTC, keep the passive vectors.
+static int OperatorAnalyseJit_B200(CeedOperator op, CeedQFunction qf, CeedInt n_in, CeedOperatorField *in, CeedInt n_out,
+                                   CeedOperatorField *out) {
+  Ceed                 ceed = CeedOperatorReturnCeed(op);
+  CeedOperator_B200   *impl;
+  CeedQFunctionField  *qf_in, *qf_out;
+  CeedInt              qf_n_in, qf_n_out, active = -1, num_roots = 0;
+  CeedElemRestriction  ru = NULL, ro = NULL;
+  CeedBasis            bu = NULL, bo = NULL;
+  CeedVector           vo;
+  b200_op_desc         d;
+  b200_jit_qfunction   j;
+  const char          *name, *source, **roots = NULL;
+  char                 dirs[4096] = "";
+  b200_ctx             ctx;
+
+  CeedCallBackend(CeedOperatorGetData(op, &impl));
+  CeedCallBackend(CeedGetB200Context(ceed, &ctx));
+  CeedCallBackend(CeedQFunctionGetFields(qf, &qf_n_in, &qf_in, &qf_n_out, &qf_out));
+  CeedCheck(n_in >= 1 && n_in <= 8 && n_out == 1, ceed, CEED_ERROR_UNSUPPORTED, "run-time compiled QFunctions: 1 to 8 inputs and one output");
+  memset(&j, 0, sizeof j);
+  j.num_inputs = n_in;
+  impl->num_passive = 0;
+  for (CeedInt i = 0; i < n_in; i++) {
+    CeedElemRestriction r;
+    CeedBasis           b;
+    CeedVector          v;
+    CeedEvalMode        mode;
+    CeedInt             size;
+
+    CeedCallBackend(FieldParts(in[i], &r, &b, &v));
+    CeedCallBackend(CeedQFunctionFieldGetSize(qf_in[i], &size));
+    CeedCallBackend(CeedQFunctionFieldGetEvalMode(qf_in[i], &mode));
+    j.input_size[i] = size;
+    if (v == CEED_VECTOR_ACTIVE) {
+      CeedCheck(active < 0 && (mode == CEED_EVAL_INTERP || mode == CEED_EVAL_GRAD), ceed, CEED_ERROR_UNSUPPORTED,
+                "run-time compiled QFunctions: one active input with CEED_EVAL_INTERP or CEED_EVAL_GRAD");
+      active    = i;
+      j.eval_in = mode == CEED_EVAL_GRAD ? B200_EVAL_GRAD : B200_EVAL_INTERP;
+      ru        = r;
+      bu        = b;
+    } else {
+      bool strided = false, backend_strides = false;
+
+      CeedCallBackend(CeedElemRestrictionIsStrided(r, &strided));
+      if (strided) CeedCallBackend(CeedElemRestrictionHasBackendStrides(r, &backend_strides));
+      CeedCheck(mode == CEED_EVAL_NONE && backend_strides && v != CEED_VECTOR_NONE, ceed, CEED_ERROR_UNSUPPORTED,
+                "run-time compiled QFunctions: passive inputs use CEED_EVAL_NONE through backend-strided restrictions");
+      impl->passive[impl->num_passive++] = v;  // reference kept until destroy
+      CeedCallBackend(CeedElemRestrictionDestroy(&r));
+      CeedCallBackend(CeedBasisDestroy(&b));
+    }
+  }
+  CeedCheck(active >= 0, ceed, CEED_ERROR_UNSUPPORTED, "run-time compiled QFunctions need an active input");
+  {
+    CeedEvalMode mode;
+
+    CeedCallBackend(FieldParts(out[0], &ro, &bo, &vo));
+    CeedCallBackend(CeedQFunctionFieldGetEvalMode(qf_out[0], &mode));
+    j.eval_out = mode == CEED_EVAL_GRAD ? B200_EVAL_GRAD : B200_EVAL_INTERP;
+    CeedCheck(vo == CEED_VECTOR_ACTIVE && ro == ru && bo == bu && (mode == CEED_EVAL_INTERP || mode == CEED_EVAL_GRAD), ceed,
+              CEED_ERROR_UNSUPPORTED, "run-time compiled QFunctions: the active output uses the active input's restriction and basis");
+  }
+  CeedCallBackend(ActiveDesc(ceed, ru, bu, &d));
+  d.qf = -1;
+  CeedCallBackend(CeedQFunctionGetKernelName(qf, &name));
+  CeedCallBackend(CeedQFunctionGetSourcePath(qf, &source));
+  CeedCallBackend(CeedGetJitSourceRoots(ceed, &num_roots, &roots));
+  for (CeedInt i = 0; i < num_roots; i++) {
+    if (strlen(dirs) + strlen(roots[i]) + 2 >= sizeof dirs) break;
+    if (dirs[0]) strcat(dirs, ":");
+    strcat(dirs, roots[i]);
+  }
+  j.source_path  = source;
+  j.name         = name;
+  j.active_input = active;
+  j.include_dirs = dirs;
+  CeedCallB200(ceed, b200_op_create_jit(ctx, &d, &j, &impl->op));
+  CeedCallBackend(CeedRestoreJitSourceRoots(ceed, &roots));
+  {
+    CeedQFunctionContext qf_ctx = NULL;
+
+    CeedCallBackend(CeedQFunctionGetContext(qf, &qf_ctx));
+    impl->ctx_size = 0;
+    if (qf_ctx) CeedCallBackend(CeedQFunctionContextGetContextSize(qf_ctx, &impl->ctx_size));
+    if (impl->ctx_size) CeedCallB200(ceed, b200_alloc(ctx, impl->ctx_size, &impl->d_ctx));
+  }
+  impl->kind = 3;
+  CeedCallBackend(CeedElemRestrictionDestroy(&ru));
+  CeedCallBackend(CeedElemRestrictionDestroy(&ro));
+  CeedCallBackend(CeedBasisDestroy(&bu));
+  CeedCallBackend(CeedBasisDestroy(&bo));
   return CEED_ERROR_SUCCESS;
 }
 
@@ -59,6 +197,11 @@ static int OperatorAnalyse_B200(CeedOperator op) {
     CeedCallBackend(CeedBasisDestroy(&bq));
     if (vx != CEED_VECTOR_ACTIVE && vx != CEED_VECTOR_NONE) CeedCallBackend(CeedVectorDestroy(&vx));
     if (vq != CEED_VECTOR_ACTIVE && vq != CEED_VECTOR_NONE) CeedCallBackend(CeedVectorDestroy(&vq));
+    CeedCallBackend(CeedQFunctionDestroy(&qf));
+    return CEED_ERROR_SUCCESS;
+  }
+  if (qf_impl->qf_kind == CEED_B200_QF_JIT) {
+    CeedCallBackend(OperatorAnalyseJit_B200(op, qf, n_in, in, n_out, out));
     CeedCallBackend(CeedQFunctionDestroy(&qf));
     return CEED_ERROR_SUCCESS;
   }
@@ -141,6 +284,21 @@ static int OperatorApplyCore_B200(CeedOperator op, CeedVector in_vec, CeedVector
   if (impl->kind == 1) {
     CeedCallBackend(CeedVectorGetDevice_B200(impl->qdata, false, &dq));
     CeedCallB200(ceed, b200_op_apply(impl->op, du, (void *)dv, dq, NULL, add ? 1 : 0));
+  } else if (impl->kind == 3) {
+    const void *passive[8] = {NULL};
+
+    for (CeedInt i = 0; i < impl->num_passive; i++) CeedCallBackend(CeedVectorGetDevice_B200(impl->passive[i], false, (const CeedScalar **)&passive[i]));
+    if (impl->ctx_size) {
+      CeedQFunction qf;
+      const void   *h_ctx;
+
+      CeedCallBackend(CeedOperatorGetQFunction(op, &qf));
+      CeedCallBackend(CeedQFunctionGetInnerContextData(qf, CEED_MEM_HOST, &h_ctx));
+      CeedCallB200(ceed, b200_copy(ctx, impl->d_ctx, h_ctx, impl->ctx_size, B200_COPY_H2D));
+      CeedCallBackend(CeedQFunctionRestoreInnerContextData(qf, &h_ctx));
+      CeedCallBackend(CeedQFunctionDestroy(&qf));
+    }
+    CeedCallB200(ceed, b200_op_apply_jit(impl->op, du, (void *)dv, passive, impl->d_ctx, add ? 1 : 0));
   } else if (impl->kind == 2) {
     CeedQFunction             qf;
     CeedQFunction_B200       *qf_impl;
@@ -182,6 +340,14 @@ static int CeedOperatorDestroy_B200(CeedOperator op) {
   CeedCallBackend(CeedOperatorGetData(op, &impl));
   if (impl->op) b200_op_destroy(impl->op);
   if (impl->qdata) CeedCallBackend(CeedVectorDestroy(&impl->qdata));
+  for (CeedInt i = 0; i < impl->num_passive; i++) CeedCallBackend(CeedVectorDestroy(&impl->passive[i]));
+  if (impl->d_ctx) {
+    Ceed     ceed = CeedOperatorReturnCeed(op);
+    b200_ctx ctx;
+
+    CeedCallBackend(CeedGetB200Context(ceed, &ctx));
+    b200_free(ctx, impl->d_ctx);
+  }
   if (impl->rstr_x) CeedCallBackend(CeedElemRestrictionDestroy(&impl->rstr_x));
   if (impl->basis_x) CeedCallBackend(CeedBasisDestroy(&impl->basis_x));
   CeedCallBackend(CeedFree(&impl));

@@ -2,9 +2,11 @@
 //
 // The pointwise kernels of this backend are compiled in: the gallery QFunctions of the hot path, recognised by kernel
 // name (MassApply, Poisson3DApply, Vector3MassApply, Vector3Poisson3DApply; Mass3DBuild and Poisson3DBuild run as the
-// geometric-factor setup).  Standalone CeedQFunctionApply on Q-vectors calls b200_qf_apply.  Other QFunctions are
-// refused with CEED_ERROR_UNSUPPORTED (no CPU fallback).  Contexts hold host data only: none of the compiled kernels
-// reads a context.
+// geometric-factor setup).  Any other QFunction created from a source file (CeedQFunctionCreateInterior with
+// "file.h:Name") is compiled at run time with NVRTC into the fused operator kernel when an operator using it is first
+// applied (b200_op_create_jit).  Standalone CeedQFunctionApply on Q-vectors calls b200_qf_apply for the gallery
+// kernels; for user QFunctions it returns CEED_ERROR_UNSUPPORTED (no CPU fallback).  Contexts hold host data; the
+// operator copies the context to the device before each run-time compiled apply.
 #include <stdlib.h>
 #include <string.h>
 
@@ -57,6 +59,12 @@ int CeedQFunctionCreate_B200(CeedQFunction qf) {
   CeedCallBackend(CeedCalloc(1, &impl));
   CeedCallBackend(CeedQFunctionGetKernelName(qf, &name));
   CeedCallBackend(QFunctionKind(name, &impl->qf_kind, &impl->build_poisson));
+  if (impl->qf_kind == -2) {
+    const char *source = NULL;
+
+    CeedCallBackend(CeedQFunctionGetSourcePath(qf, &source));
+    if (source && source[0]) impl->qf_kind = CEED_B200_QF_JIT;
+  }
   CeedCallBackend(CeedQFunctionSetData(qf, impl));
   CeedCallBackend(CeedSetBackendFunction(ceed, "QFunction", qf, "Apply", CeedQFunctionApply_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "QFunction", qf, "Destroy", CeedQFunctionDestroy_B200));

@@ -1,13 +1,83 @@
-// Drop-in check of `/gpu/cuda/b200` through the stock libCEED API: the same Poisson problem (gallery Poisson3DBuild +
-// Poisson3DApply on a perturbed box of hexahedra) is set up on `/gpu/cuda/b200` and on `/cpu/self/ref/serial` in one
-// process, and the two applies are compared (relative l-infinity, tolerance 1e-12).  Needs a GPU and a libCEED build;
-// prints nothing on success, like the reference's tests/t*.c.
+// Drop-in check of `/gpu/cuda/b200` through the stock libCEED API: the same problems are set up on `/gpu/cuda/b200`
+// and on `/cpu/self/ref/serial` in one process and the applies compared (relative l-infinity, tolerance 1e-12):
+//   1. gallery Poisson3DBuild + Poisson3DApply on a perturbed box of hexahedra (fused compiled kernel);
+//   2. gallery Mass3DBuild + the user QFunction ScaledMass from tests/qfunctions/user-qfunctions.h with a context
+//      (NVRTC-compiled on /gpu/cuda/b200, the function pointer on the CPU backend).
+// Needs a GPU and a libCEED build; prints nothing on success, like the reference's tests/t*.c.
 #include <ceed.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 
+#include "user-qfunctions.h"
+
 int CeedB200Register(void);
+
+static void ApplyUserMass(const char *resource, int n, int P, const double *coords, const CeedInt *xoff, const CeedInt *uoff, const double *u,
+                          double *v) {
+  const int            Q = P + 1, ne = n * n * n, nv = (n + 1) * (n + 1) * (n + 1), nd = n * (P - 1) + 1, N = nd * nd * nd;
+  Ceed                 ceed;
+  CeedVector           X, U, V, QD;
+  CeedBasis            bx, bu;
+  CeedElemRestriction  rx, ru, rq;
+  CeedQFunction        qf_b, qf_a;
+  CeedQFunctionContext qctx;
+  CeedOperator         op_b, op_a;
+  struct ScaledMassContext c = {0.75};
+
+  CeedInit(resource, &ceed);
+  CeedElemRestrictionCreate(ceed, ne, 8, 3, nv, 3 * nv, CEED_MEM_HOST, CEED_COPY_VALUES, xoff, &rx);
+  CeedElemRestrictionCreate(ceed, ne, P * P * P, 1, 1, N, CEED_MEM_HOST, CEED_COPY_VALUES, uoff, &ru);
+  CeedElemRestrictionCreateStrided(ceed, ne, Q * Q * Q, 1, ne * Q * Q * Q, CEED_STRIDES_BACKEND, &rq);
+  CeedBasisCreateTensorH1Lagrange(ceed, 3, 3, 2, Q, CEED_GAUSS, &bx);
+  CeedBasisCreateTensorH1Lagrange(ceed, 3, 1, P, Q, CEED_GAUSS, &bu);
+  CeedVectorCreate(ceed, 3 * nv, &X);
+  CeedVectorSetArray(X, CEED_MEM_HOST, CEED_COPY_VALUES, (double *)coords);
+  CeedVectorCreate(ceed, ne * Q * Q * Q, &QD);
+  CeedVectorCreate(ceed, N, &U);
+  CeedVectorCreate(ceed, N, &V);
+  CeedVectorSetArray(U, CEED_MEM_HOST, CEED_COPY_VALUES, (double *)u);
+  CeedQFunctionCreateInteriorByName(ceed, "Mass3DBuild", &qf_b);
+  CeedOperatorCreate(ceed, qf_b, CEED_QFUNCTION_NONE, CEED_QFUNCTION_NONE, &op_b);
+  CeedOperatorSetField(op_b, "dx", rx, bx, CEED_VECTOR_ACTIVE);
+  CeedOperatorSetField(op_b, "weights", CEED_ELEMRESTRICTION_NONE, bx, CEED_VECTOR_NONE);
+  CeedOperatorSetField(op_b, "qdata", rq, CEED_BASIS_NONE, CEED_VECTOR_ACTIVE);
+  CeedOperatorApply(op_b, X, QD, CEED_REQUEST_IMMEDIATE);
+  CeedQFunctionCreateInterior(ceed, 1, ScaledMass, USER_QF_PATH ":ScaledMass", &qf_a);
+  CeedQFunctionAddInput(qf_a, "qdata", 1, CEED_EVAL_NONE);
+  CeedQFunctionAddInput(qf_a, "u", 1, CEED_EVAL_INTERP);
+  CeedQFunctionAddOutput(qf_a, "v", 1, CEED_EVAL_INTERP);
+  CeedQFunctionContextCreate(ceed, &qctx);
+  CeedQFunctionContextSetData(qctx, CEED_MEM_HOST, CEED_COPY_VALUES, sizeof c, &c);
+  CeedQFunctionSetContext(qf_a, qctx);
+  CeedOperatorCreate(ceed, qf_a, CEED_QFUNCTION_NONE, CEED_QFUNCTION_NONE, &op_a);
+  CeedOperatorSetField(op_a, "qdata", rq, CEED_BASIS_NONE, QD);
+  CeedOperatorSetField(op_a, "u", ru, bu, CEED_VECTOR_ACTIVE);
+  CeedOperatorSetField(op_a, "v", ru, bu, CEED_VECTOR_ACTIVE);
+  CeedOperatorApply(op_a, U, V, CEED_REQUEST_IMMEDIATE);
+  {
+    const double *a;
+
+    CeedVectorGetArrayRead(V, CEED_MEM_HOST, &a);
+    for (int i = 0; i < N; i++) v[i] = a[i];
+    CeedVectorRestoreArrayRead(V, &a);
+  }
+  CeedOperatorDestroy(&op_a);
+  CeedOperatorDestroy(&op_b);
+  CeedQFunctionContextDestroy(&qctx);
+  CeedQFunctionDestroy(&qf_a);
+  CeedQFunctionDestroy(&qf_b);
+  CeedElemRestrictionDestroy(&rx);
+  CeedElemRestrictionDestroy(&ru);
+  CeedElemRestrictionDestroy(&rq);
+  CeedBasisDestroy(&bx);
+  CeedBasisDestroy(&bu);
+  CeedVectorDestroy(&X);
+  CeedVectorDestroy(&U);
+  CeedVectorDestroy(&V);
+  CeedVectorDestroy(&QD);
+  CeedDestroy(&ceed);
+}
 
 static void Apply(const char *resource, int n, int P, const double *coords, const CeedInt *xoff, const CeedInt *uoff, const double *u, double *v) {
   const int     Q = P + 1, ne = n * n * n, nv = (n + 1) * (n + 1) * (n + 1), nd = n * (P - 1) + 1, N = nd * nd * nd;
@@ -94,6 +164,13 @@ int main(void) {
   double err = 0, scale = 0;
   for (int i = 0; i < N; i++) err = fmax(err, fabs(v_gpu[i] - v_ref[i])), scale = fmax(scale, fabs(v_ref[i]));
   if (err > 1e-12 * scale) printf("Error: /gpu/cuda/b200 differs from /cpu/self/ref/serial by %e (relative)\n", err / scale);
+  int fail = err > 1e-12 * scale;
+  ApplyUserMass("/gpu/cuda/b200", n, P, coords, xoff, uoff, u, v_gpu);
+  ApplyUserMass("/cpu/self/ref/serial", n, P, coords, xoff, uoff, u, v_ref);
+  err = 0, scale = 0;
+  for (int i = 0; i < N; i++) err = fmax(err, fabs(v_gpu[i] - v_ref[i])), scale = fmax(scale, fabs(v_ref[i]));
+  if (err > 1e-12 * scale) printf("Error: user QFunction on /gpu/cuda/b200 differs from /cpu/self/ref/serial by %e (relative)\n", err / scale);
+  fail |= err > 1e-12 * scale;
   free(coords), free(u), free(v_gpu), free(v_ref), free(xoff), free(uoff);
-  return err > 1e-12 * scale;
+  return fail;
 }
