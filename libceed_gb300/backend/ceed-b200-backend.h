@@ -49,13 +49,15 @@ typedef struct {
   b200_op     op;
   int         kind;  // 0 not analysed, 1 fused apply, 2 geometric-factor build, 3 run-time compiled QFunction, -1 unsupported
   CeedVector  qdata, kappa;
-  CeedElemRestriction rstr_u, rstr_x;
+  CeedElemRestriction rstr_u, rstr_x;  // rstr_u: active restriction of the fused apply (diagonal assembly)
   CeedBasis   basis_x;
   // kind 3: passive inputs in QFunction order (without the active one) and the device copy of the context
   CeedInt     num_passive;
   CeedVector  passive[8];
   void       *d_ctx;
   size_t      ctx_size;
+  int         qf_kind;  // kind 1: B200_QF_* of the fused apply
+  b200_op_desc desc;    // kind 1: the fused operator's descriptor (diagonal assembly)
 } CeedOperator_B200;
 
 CEED_INTERN int CeedVectorCreate_B200(CeedSize n, CeedVector vec);

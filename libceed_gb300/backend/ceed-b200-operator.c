@@ -257,8 +257,11 @@ static int OperatorAnalyse_B200(CeedOperator op) {
       d.grad_1d     = grad;
     }
     CeedCallB200(ceed, b200_op_create(ctx, &d, &impl->op));
-    impl->qdata = vq;  // reference kept until destroy
-    impl->kind  = 1;
+    impl->qdata   = vq;  // reference kept until destroy
+    impl->kind    = 1;
+    impl->qf_kind = qf_impl->qf_kind;
+    impl->desc    = d;
+    CeedCallBackend(CeedElemRestrictionReferenceCopy(ru, &impl->rstr_u));
     CeedCallBackend(CeedElemRestrictionDestroy(&ru));
     CeedCallBackend(CeedElemRestrictionDestroy(&rq));
     CeedCallBackend(CeedElemRestrictionDestroy(&ro));
@@ -334,6 +337,46 @@ static int CeedOperatorApplyAdd_B200(CeedOperator op, CeedVector in_vec, CeedVec
   return OperatorApplyCore_B200(op, in_vec, out_vec, true);
 }
 
+// CeedOperatorLinearAssembleAddDiagonal (interface/ceed-preconditioning.c:2395) for the fused gallery operators:
+// diag += the operator's diagonal, by b200_assemble_diagonal (deterministic through the restriction's inverse-offset
+// plan when the Ceed is deterministic).
+static int CeedOperatorLinearAssembleAddDiagonal_B200(CeedOperator op, CeedVector assembled, CeedRequest *request) {
+  Ceed                      ceed = CeedOperatorReturnCeed(op);
+  CeedOperator_B200        *impl;
+  CeedElemRestriction_B200 *r_impl;
+  const CeedScalar         *dq, *dd;
+  b200_ctx                  ctx;
+  void                     *tmp = NULL;
+  bool                      det;
+  int                       poisson;
+
+  (void)request;
+  CeedCallBackend(OperatorAnalyse_B200(op));
+  CeedCallBackend(CeedOperatorGetData(op, &impl));
+  CeedCheck(impl->kind == 1, ceed, CEED_ERROR_UNSUPPORTED, "diagonal assembly on /gpu/cuda/b200 covers the fused gallery operators");
+  CeedCallBackend(CeedGetB200Context(ceed, &ctx));
+  CeedCallBackend(CeedIsDeterministic(ceed, &det));
+  CeedCallBackend(CeedElemRestrictionGetData(impl->rstr_u, &r_impl));
+  const b200_op_desc *d = &impl->desc;
+  if (det && !r_impl->plan) {
+    CeedInt elem_size;
+
+    CeedCallBackend(CeedElemRestrictionGetElementSize(impl->rstr_u, &elem_size));
+    CeedCallB200(ceed, b200_plan_create(ctx, d->num_elem, elem_size, d->num_comp, d->comp_stride, d->l_size, r_impl->h_offsets, r_impl->d_offsets,
+                                        &r_impl->plan));
+  }
+  poisson = impl->qf_kind == B200_QF_POISSON || impl->qf_kind == B200_QF_VECPOISSON;
+  CeedCallBackend(CeedVectorGetDevice_B200(impl->qdata, false, &dq));
+  CeedCallBackend(CeedVectorGetDevice_B200(assembled, true, &dd));
+  CeedCallB200(ceed, b200_alloc(ctx, sizeof(double) * (size_t)d->l_size, &tmp));
+  int st = b200_assemble_diagonal(ctx, poisson, d->P_1d, d->Q_1d, d->num_elem, d->num_comp, d->comp_stride, d->l_size, d->interp_1d, d->grad_1d,
+                                  d->offsets, dq, NULL, (double *)tmp, det ? r_impl->plan : NULL);
+  if (!st) st = b200_vec_axpy(ctx, B200_F64, d->l_size, 1.0, tmp, (void *)dd);
+  b200_free(ctx, tmp);
+  CeedCheck(!st, ceed, CEED_ERROR_BACKEND, "b200_assemble_diagonal: %s", b200_last_error());
+  return CEED_ERROR_SUCCESS;
+}
+
 static int CeedOperatorDestroy_B200(CeedOperator op) {
   CeedOperator_B200 *impl;
 
@@ -349,6 +392,7 @@ static int CeedOperatorDestroy_B200(CeedOperator op) {
     b200_free(ctx, impl->d_ctx);
   }
   if (impl->rstr_x) CeedCallBackend(CeedElemRestrictionDestroy(&impl->rstr_x));
+  if (impl->rstr_u) CeedCallBackend(CeedElemRestrictionDestroy(&impl->rstr_u));
   if (impl->basis_x) CeedCallBackend(CeedBasisDestroy(&impl->basis_x));
   CeedCallBackend(CeedFree(&impl));
   return CEED_ERROR_SUCCESS;
@@ -363,6 +407,7 @@ int CeedOperatorCreate_B200(CeedOperator op) {
   CeedCallBackend(CeedOperatorSetData(op, impl));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "Apply", CeedOperatorApply_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "ApplyAdd", CeedOperatorApplyAdd_B200));
+  CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "LinearAssembleAddDiagonal", CeedOperatorLinearAssembleAddDiagonal_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Operator", op, "Destroy", CeedOperatorDestroy_B200));
   CeedCallBackend(CeedDestroy(&ceed));
   return CEED_ERROR_SUCCESS;

@@ -1,6 +1,7 @@
 // Drop-in check of `/gpu/cuda/b200` through the stock libCEED API: the same problems are set up on `/gpu/cuda/b200`
 // and on `/cpu/self/ref/serial` in one process and the applies compared (relative l-infinity, tolerance 1e-12):
 //   1. gallery Poisson3DBuild + Poisson3DApply on a perturbed box of hexahedra (fused compiled kernel);
+//      and its assembled diagonal (CeedOperatorLinearAssembleDiagonal);
 //   2. gallery Mass3DBuild + the user QFunction ScaledMass from tests/qfunctions/user-qfunctions.h with a context
 //      (NVRTC-compiled on /gpu/cuda/b200, the function pointer on the CPU backend).
 // Needs a GPU and a libCEED build; prints nothing on success, like the reference's tests/t*.c.
@@ -79,7 +80,8 @@ static void ApplyUserMass(const char *resource, int n, int P, const double *coor
   CeedDestroy(&ceed);
 }
 
-static void Apply(const char *resource, int n, int P, const double *coords, const CeedInt *xoff, const CeedInt *uoff, const double *u, double *v) {
+static void Apply(const char *resource, int n, int P, const double *coords, const CeedInt *xoff, const CeedInt *uoff, const double *u, double *v,
+                  double *diag) {
   const int     Q = P + 1, ne = n * n * n, nv = (n + 1) * (n + 1) * (n + 1), nd = n * (P - 1) + 1, N = nd * nd * nd;
   Ceed          ceed;
   CeedVector    X, U, V, QD;
@@ -117,6 +119,14 @@ static void Apply(const char *resource, int n, int P, const double *coords, cons
 
     CeedVectorGetArrayRead(V, CEED_MEM_HOST, &a);
     for (int i = 0; i < N; i++) v[i] = a[i];
+    CeedVectorRestoreArrayRead(V, &a);
+  }
+  CeedOperatorLinearAssembleDiagonal(op_a, V, CEED_REQUEST_IMMEDIATE);
+  {
+    const double *a;
+
+    CeedVectorGetArrayRead(V, CEED_MEM_HOST, &a);
+    for (int i = 0; i < N; i++) diag[i] = a[i];
     CeedVectorRestoreArrayRead(V, &a);
   }
   CeedOperatorDestroy(&op_a);
@@ -159,12 +169,18 @@ int main(void) {
   }
   for (int i = 0; i < N; i++) u[i] = sin(0.37 * i);
   CeedB200Register();
-  Apply("/gpu/cuda/b200", n, P, coords, xoff, uoff, u, v_gpu);
-  Apply("/cpu/self/ref/serial", n, P, coords, xoff, uoff, u, v_ref);
+  double *d_gpu = malloc(sizeof(double) * N), *d_ref = malloc(sizeof(double) * N);
+  Apply("/gpu/cuda/b200", n, P, coords, xoff, uoff, u, v_gpu, d_gpu);
+  Apply("/cpu/self/ref/serial", n, P, coords, xoff, uoff, u, v_ref, d_ref);
   double err = 0, scale = 0;
   for (int i = 0; i < N; i++) err = fmax(err, fabs(v_gpu[i] - v_ref[i])), scale = fmax(scale, fabs(v_ref[i]));
   if (err > 1e-12 * scale) printf("Error: /gpu/cuda/b200 differs from /cpu/self/ref/serial by %e (relative)\n", err / scale);
   int fail = err > 1e-12 * scale;
+  err = 0, scale = 0;
+  for (int i = 0; i < N; i++) err = fmax(err, fabs(d_gpu[i] - d_ref[i])), scale = fmax(scale, fabs(d_ref[i]));
+  if (err > 1e-12 * scale) printf("Error: assembled diagonal on /gpu/cuda/b200 differs by %e (relative)\n", err / scale);
+  fail |= err > 1e-12 * scale;
+  free(d_gpu), free(d_ref);
   ApplyUserMass("/gpu/cuda/b200", n, P, coords, xoff, uoff, u, v_gpu);
   ApplyUserMass("/cpu/self/ref/serial", n, P, coords, xoff, uoff, u, v_ref);
   err = 0, scale = 0;
