@@ -77,6 +77,11 @@ int b200_ctx_sync(b200_ctx ctx);
 int b200_ctx_destroy(b200_ctx ctx);
 /* Number of kernels this library launched on the context (all entry points). */
 int b200_ctx_launch_count(b200_ctx ctx, int64_t *count);
+/* Device status word of the context, read and cleared (synchronizes the stream).  0, or an OR of B200_STATUS_* bits
+ * set by kernels whose bounded wait on an asynchronous copy gave up (their results are then invalid).  No counterpart
+ * in the reference (its kernels do not wait on asynchronous copies). */
+enum { B200_STATUS_COPY_TIMEOUT = 1 };
+int b200_ctx_status(b200_ctx ctx, int *status);
 
 /* ---- Device memory of CeedVector arrays.  Replaces the device half of CeedVectorCreate_Cuda / SetArray /
  *      SyncArray (backends/cuda-ref/ceed-cuda-ref-vector.c:97-262). ------------------------------------------------ */
@@ -157,7 +162,8 @@ typedef struct {
   const double  *interp_1d;   /* host, Q x P */
   const double  *grad_1d;     /* host, Q x P */
   int            elems_per_block; /* 0: tuned default */
-  int            staging;         /* 0: default, 1: registers, 2: shared memory, 3: persistent pipelined */
+  int            staging;         /* 0: default, 1: registers, 2: shared memory, 3: persistent pipelined,
+                                     4: point (Q^3-thread) mapping, 5: bulk-copy (TMA) qdata slabs */
 } b200_op_desc;
 
 int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);

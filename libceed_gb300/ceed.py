@@ -95,6 +95,12 @@ class Ceed:
         call("b200_ctx_launch_count", self._ctx, ctypes.byref(n))
         return n.value
 
+    def status(self):
+        """Read and clear the device status word (B200_STATUS_* bits; 0 when every bounded wait completed)."""
+        st = ctypes.c_int()
+        call("b200_ctx_status", self._ctx, ctypes.byref(st))
+        return st.value
+
     def fma_peak(self, prec=F64):
         """Measured fused multiply-add rate of the FP64 or FP32 pipe (TFLOP/s), the compute roofline's denominator."""
         t = ctypes.c_double()

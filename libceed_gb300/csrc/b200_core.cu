@@ -87,6 +87,8 @@ extern "C" int b200_ctx_create(int device_id, b200_ctx *out) {
   ctx->red_blocks = reduce_blocks(ctx->num_sms);
   B200_CUDA(cudaMalloc(&ctx->red_partial, sizeof(double) * (size_t)(2 * ctx->red_blocks + 8)));
   B200_CUDA(cudaMallocHost(&ctx->red_result_host, sizeof(double) * 8));
+  B200_CUDA(cudaMalloc(&ctx->d_status, sizeof(int)));
+  B200_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
   *out = ctx;
   return B200_SUCCESS;
 }
@@ -111,9 +113,19 @@ extern "C" int b200_ctx_launch_count(b200_ctx ctx, int64_t *count) {
   return B200_SUCCESS;
 }
 
+extern "C" int b200_ctx_status(b200_ctx ctx, int *status) {
+  int h = 0;
+  B200_CUDA(cudaMemcpyAsync(&h, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  B200_CUDA(cudaStreamSynchronize(ctx->stream));
+  B200_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+  *status = h;
+  return B200_SUCCESS;
+}
+
 extern "C" int b200_ctx_destroy(b200_ctx ctx) {
   if (!ctx) return B200_SUCCESS;
   cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_status);
   cudaFree(ctx->red_partial);
   cudaFreeHost(ctx->red_result_host);
   delete ctx;

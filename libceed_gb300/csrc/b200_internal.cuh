@@ -19,6 +19,7 @@ struct b200_ctx_s {
   double      *red_partial;
   double      *red_result_host;  // pinned
   int          red_blocks;
+  int         *d_status;  // device: kernels OR in B200_STATUS_* bits (a bounded wait that gave up)
 };
 
 namespace b200 {

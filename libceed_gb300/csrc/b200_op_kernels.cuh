@@ -25,6 +25,10 @@
 //   k_op_apply_pipe            persistent blocks looping over element batches with a two-deep software pipeline:
 //                              while batch i is computed, batch i+1's qdata streams into a second shared-memory buffer
 //                              (cp.async) and its u values and batch i+2's offsets are loaded into registers.
+//   k_op_apply<.., kStageTma>  the block's elements are consecutive, so each qdata component of the block is one
+//                              contiguous range: one thread issues one cp.async.bulk per component at entry, completing
+//                              on an mbarrier that the threads wait on (bounded) just before the pointwise stage, so the
+//                              copy overlaps the gather and the interpolation without registers or load instructions.
 //   k_op_apply_3d              "point" mapping: a team of Q^3 threads per element, one thread per output point of
 //                              each stage (Q*P*P, Q*Q*P, Q^3, ... threads active), the 1D matrices in shared memory
 //                              and the thread's own qdata in registers (one coalesced load per component).
@@ -39,7 +43,8 @@
 
 namespace b200 {
 
-enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4 };  // kStage3D: point mapping (k_op_apply_3d)
+// kStage3D: point mapping (k_op_apply_3d); kStageTma: the block's qdata slabs arrive by bulk copy (TMA engine)
+enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4, kStageTma = 5 };
 
 // Shared-memory layout of an element tile: point (x, y, z) at x + Q*y + tile_plane(Q)*z, three tiles per team
 // (tile_buf each), and a team stride that is fixed modulo 32 words.  The plane padding and the team stride residue
@@ -92,6 +97,7 @@ struct OpArgs {
   T             *e_out;  // E-vector [comp][elem][node] (deterministic scatter)
   const T       *qdata;  // [qcomp][elem][qpt]
   const T       *kappa;  // [elem][qpt] or nullptr
+  int           *status; // device status word (B200_STATUS_* bits)
 };
 
 template <int QF>
@@ -111,6 +117,51 @@ struct OpShape {
   static constexpr int extra     = (STAGE == kStageSmem ? QFTraits<QF>::nqk * Q3 : 0) +
                                (STAGE == kStagePipe ? 2 * QFTraits<QF>::nqk * Q3 + (P3 * 4 + (int)sizeof(T) - 1) / (int)sizeof(T) : 0);
   static constexpr int team_smem = tile_team_stride(Q, extra);
+};
+
+// ---- bulk copies (TMA engine) completing on an mbarrier ---------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // make the initialised barrier visible to the copy engine
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// dst (shared) and src (global) 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(smem_addr(dst)), "l"(src),
+               "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+// Wait for phase `parity` of the barrier to complete, giving up after a bounded number of polls (each try_wait also
+// suspends for a bounded time).  Returns false on give-up.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  for (int i = 0; i < (1 << 22); i++) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Shared-memory prefix of the bulk-copy staging: an mbarrier (16 bytes) and one slab per staged qdata component of
+// epb*Q^3 storage values plus 16 bytes of alignment slack on each side.
+template <typename S, int Q3>
+__host__ __device__ constexpr size_t tma_slab_bytes(int epb) {
+  return ((size_t)epb * Q3 * sizeof(S) + 32 + 15) / 16 * 16;
+}
+template <typename S, int Q3, int NQK>
+__host__ __device__ constexpr size_t tma_prefix_bytes(int epb) {
+  return 16 + NQK * tma_slab_bytes<S, Q3>(epb);
+}
+
+struct NoWait {
+  __device__ void operator()() const {}
 };
 
 // out[j] = sum_k M[j*K + k] in[k], j < J
@@ -203,8 +254,8 @@ struct Contract {
 // values (x, y, z < P) and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata
 // component k (kappa already applied) at point (a, b, z).  On exit, threads with a, b < P hold in out[p] the element
 // result at node (p, a, b).  Uses s0, s1, s2 (Q^3 each) and block-wide barriers.
-template <typename T, int P, int Q, int QF, bool EO, typename QD>
-__device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P, Q> &M, int a, int b, QD qd, T (&out)[P]) {
+template <typename T, int P, int Q, int QF, bool EO, typename QD, typename QW = NoWait>
+__device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P, Q> &M, int a, int b, QD qd, T (&out)[P], QW qwait = QW{}) {
   using C             = Contract<T, P, Q, EO>;
   constexpr bool GRAD = QFTraits<QF>::grad;
   // ---- X interpolation: lines (y, z) < P --------------------------------------------------------------------------
@@ -257,6 +308,7 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
     }
     __syncthreads();
     // ---- pointwise QFunction on the z-line (x = a, y = b) ------------------------------------------------------------
+    qwait();
 #pragma unroll
     for (int z = 0; z < Q; z++) {
       T D[6];
@@ -303,6 +355,7 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
     // ---- mass: pointwise product on the z-line, then Z interpolation transposed ----------------------------------------
     // Each thread reads and rewrites only its own z-line of s0, so no barrier is needed here.
     T w[Q], o[P];
+    qwait();
 #pragma unroll
     for (int z = 0; z < Q; z++) w[z] = U[z] * qd(0, z);
     C::interp_t(M, w, o);
@@ -357,12 +410,16 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   const int64_t e      = (int64_t)blockIdx.x * args.epb + slot;
   const bool    active = e < args.num_elem;
   const int64_t ne     = args.num_elem;
-  T *s0 = reinterpret_cast<T *>(smem_raw) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q), *sq = s2 + tile_buf(Q);
+  using S              = typename Store<T>::type;
+  constexpr int NQK    = TR::nqk;
+  // Bulk-copy staging: [mbarrier][NQK slabs][team tiles]; the other stagings start with the team tiles.
+  const size_t       prefix = STAGE == kStageTma ? tma_prefix_bytes<S, Q3, NQK>(args.epb) : 0;
+  unsigned long long *bar   = reinterpret_cast<unsigned long long *>(smem_raw);
+  T *s0 = reinterpret_cast<T *>(smem_raw + prefix) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q), *sq = s2 + tile_buf(Q);
 
   // ---- qdata staging ------------------------------------------------------------------------------------------------
   // Register staging keeps the loaded storage values (S) and converts at first use, so that the loads stay in flight
   // through the interpolation stages also when T is not the storage type.
-  using S          = typename Store<T>::type;
   constexpr int RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1;
   S             rq[RQ][RZ];
   if constexpr (STAGE == kStageReg) {
@@ -377,7 +434,7 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
         if constexpr (TR::kappa) rq[k][z] *= kap;
       }
     }
-  } else {
+  } else if constexpr (STAGE == kStageSmem) {
     for (int i = tid; i < NQD * Q3; i += Q2) {
       const int k = i / Q3, q = i % Q3;
       sq[i]       = active ? T(args.qdata[((int64_t)k * ne + e) * Q3 + q]) : T(0);
@@ -385,9 +442,49 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     if constexpr (TR::kappa)
       for (int q = tid; q < Q3; q += Q2) sq[NQD * Q3 + q] = active ? T(args.kappa[e * Q3 + q]) : T(0);
   }
+  // Bulk-copy staging: slab k holds component k (kappa last) of the block's elements e0 .. e0 + nb - 1.  A range that
+  // does not start or end on 16 bytes is widened to the enclosing 16-byte chunks (each chunk holds array data, so it
+  // lies on a mapped page); qoff[k] is the offset, in storage values, of element e0 within slab k.
+  const int64_t e0   = (int64_t)blockIdx.x * args.epb;
+  const int     nb   = (int)((ne - e0) < args.epb ? (ne - e0) : args.epb);
+  const size_t  slab = tma_slab_bytes<S, Q3>(args.epb);
+  int           qoff[STAGE == kStageTma ? NQK : 1];
+  if constexpr (STAGE == kStageTma) {
+#pragma unroll
+    for (int k = 0; k < NQK; k++) {
+      const S *src = (TR::kappa && k == NQD) ? args.kappa + e0 * Q3 : args.qdata + ((int64_t)k * ne + e0) * Q3;
+      qoff[k]      = (int)(((size_t)src & 15) / sizeof(S));
+    }
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      unsigned total = 0;
+      for (int k = 0; k < NQK; k++) {
+        const S     *src = (TR::kappa && k == NQD) ? args.kappa + e0 * Q3 : args.qdata + ((int64_t)k * ne + e0) * Q3;
+        const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
+        total += (unsigned)(hi - lo);
+      }
+      mbar_arrive_expect_tx(bar, total);
+      for (int k = 0; k < NQK; k++) {
+        const S     *src = (TR::kappa && k == NQD) ? args.kappa + e0 * Q3 : args.qdata + ((int64_t)k * ne + e0) * Q3;
+        const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
+        bulk_copy_g2s(smem_raw + 16 + k * slab, (const void *)lo, (unsigned)(hi - lo), bar);
+      }
+    }
+  }
+  auto qwait = [&]() {
+    if constexpr (STAGE == kStageTma) {
+      if (!mbar_wait(bar, 0) && threadIdx.x == 0) atomicOr(args.status, B200_STATUS_COPY_TIMEOUT);
+    }
+  };
   auto qd = [&](int k, int z) -> T {
     if constexpr (STAGE == kStageReg) return T(rq[k][z]);
-    else {
+    else if constexpr (STAGE == kStageTma) {
+      const S  *sl  = reinterpret_cast<const S *>(smem_raw + 16);
+      const int q   = slot * Q3 + B200_QLIN(a, b, z);
+      const int st  = (int)(slab / sizeof(S));
+      if constexpr (TR::kappa) return T(sl[k * st + qoff[k] + q] * sl[NQD * st + qoff[NQD] + q]);
+      else return T(sl[k * st + qoff[k] + q]);
+    } else {
       const int q = B200_QLIN(a, b, z);
       if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];
       else return sq[k * Q3 + q];
@@ -403,7 +500,8 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     }
     __syncthreads();
     T out[P];
-    op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out);
+    if (c == 0) op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out, qwait);
+    else op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out);
     if (a < P && b < P && active) scatter_line<T, P>(args, e, c, args.offsets + e * P3 + P * (a + P * b), a, b, out);
   }
 }

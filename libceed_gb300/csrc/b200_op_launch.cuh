@@ -11,7 +11,7 @@ namespace b200 {
 constexpr int kOpPMin = 2, kOpPMax = 9;  // compiled range of P_1d (Q_1d = P_1d + 1)
 
 // Kernel variants: qdata staging x contraction form.
-enum { kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kVar3D = 5, kNumVariants = 6 };
+enum { kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kVar3D = 5, kVarTma = 6, kVarTmaEO = 7, kNumVariants = 8 };
 
 // Untyped launch request; pointers are reinterpreted in the instance's precision.
 struct OpLaunch {
@@ -22,6 +22,7 @@ struct OpLaunch {
   const void    *u, *qdata, *kappa, *w;  // w: second field of the kappa gradient
   void          *v, *e_out, *g;
   const double  *B, *G;  // host 1D matrices, Q x P and Q x Q
+  int           *status;  // device status word of the context
 };
 
 using OpLauncher  = int (*)(b200_ctx ctx, const OpLaunch &req);
@@ -85,12 +86,16 @@ inline OpArgs<typename Store<T>::type> make_args(const OpLaunch &r) {
   a.e_out       = (S *)r.e_out;
   a.qdata       = (const S *)r.qdata;
   a.kappa       = (const S *)r.kappa;
+  a.status      = r.status;
   return a;
 }
 
 template <typename T, int P, int QF, int STAGE>
 size_t op_smem(int epb) {
-  return sizeof(T) * (size_t)epb * OpShape<T, P, P + 1, QF, STAGE>::team_smem;
+  constexpr int Q = P + 1;
+  size_t        prefix = 0;
+  if constexpr (STAGE == kStageTma) prefix = tma_prefix_bytes<typename Store<T>::type, Q * Q * Q, QFTraits<QF>::nqk>(epb);
+  return prefix + sizeof(T) * (size_t)epb * OpShape<T, P, Q, QF, STAGE>::team_smem;
 }
 
 template <typename K>
@@ -201,6 +206,7 @@ bool op_variant(int variant, OpInstance *out) {
     // Float-float: only the even-odd kernels (half the multiply-adds, which cost ~15 FP32 operations each).
     if (variant == kVarRegEO) *out = op_instance<T, P, QF, kStageReg, true>();
     else if (variant == kVarSmemEO) *out = op_instance<T, P, QF, kStageSmem, true>();
+    else if (variant == kVarTmaEO) *out = op_instance<T, P, QF, kStageTma, true>();
     else return false;
     return true;
   } else {
@@ -217,6 +223,8 @@ bool op_variant(int variant, OpInstance *out) {
           return false;
         }
       case kVar3D: *out = op_instance_3d<T, P, QF>(); return true;
+      case kVarTma: *out = op_instance<T, P, QF, kStageTma, false>(); return true;
+      case kVarTmaEO: *out = op_instance<T, P, QF, kStageTma, true>(); return true;
       default: return false;
     }
   }

@@ -149,6 +149,8 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
     *variant = kVarPipeEO;
   } else if (stage == kStage3D) {
     *variant = kVar3D;
+  } else if (stage == kStageTma) {
+    *variant = eo ? kVarTmaEO : kVarTma;
   } else {
     B200_CHECK(false, B200_ERROR_UNSUPPORTED, "unknown qdata staging %d", stage);
   }
@@ -295,6 +297,7 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   r.e_out       = op->e_work;
   r.B           = op->B.data();
   r.G           = op->Gc.data();
+  r.status      = ctx->d_status;
   if (!r.det && !add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
   int st = op->inst.launch(ctx, r);
   if (st) return st;
@@ -322,6 +325,7 @@ extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, cons
   r.g       = g;
   r.B       = op->B.data();
   r.G       = op->Gc.data();
+  r.status  = ctx->d_status;
   return launch(ctx, r);
 }
 
@@ -472,7 +476,8 @@ extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void 
     const void    *u;
     void          *v, *e_out;
     const void    *qdata, *kappa;
-  } a{d.num_elem, d.comp_stride, op->epb, d.scatter == B200_SCATTER_DETERMINISTIC, d.offsets, u, v, op->e_work, nullptr, nullptr};
+    int           *status;
+  } a{d.num_elem, d.comp_stride, op->epb, d.scatter == B200_SCATTER_DETERMINISTIC, d.offsets, u, v, op->e_work, nullptr, nullptr, ctx->d_status};
   static_assert(sizeof(ArgsBlob) == sizeof(OpArgs<double>), "argument layout");
   struct FieldsBlob {
     const void *passive[kJitMaxFieldsHost];

@@ -28,7 +28,7 @@ def ceed_det():
 
 @pytest.mark.parametrize("case", ["poisson_n6_p1", "poisson_n4_p2", "poisson_n3_p3", "poisson_n3_p4", "poisson_n2_p5", "poisson_n2_p6",
                                   "poisson_n2_p7", "poisson_n2_p8", "mass_n8_p3"])
-@pytest.mark.parametrize("staging", [1, 2])
+@pytest.mark.parametrize("staging", [1, 2, 5])
 @pytest.mark.parametrize("epb", [0, 3])
 def test_float_float_apply_matches_reference(ceed, ceed_det, case, staging, epb):
     for c in (ceed, ceed_det):
@@ -43,6 +43,7 @@ def test_float_float_apply_matches_reference(ceed, ceed_det, case, staging, epb)
         op.apply(u, v)
         assert relinf(v.get_array_read(), g["v"]) < 1e-12
         assert op.fused(lc.F64X).tile()[2] == staging
+        assert c.status() == 0
 
 
 @pytest.mark.parametrize("p", [2, 4, 6])

@@ -46,12 +46,13 @@ def test_fp64_apply_matches_reference(ceed, ceed_det, case, det):
 
 
 @pytest.mark.parametrize("case", ["poisson_n3_p4", "poisson_n6_p1", "poisson_n2_p8", "mass_n8_p3", "kappa_n3_p3", "vpoisson_n4_p2"])
-@pytest.mark.parametrize("staging", [1, 2, 3, 4])
+@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("epb", [1, 3])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_every_kernel_variant(ceed, ceed_det, case, staging, epb, dtype):
-    """Register, shared-memory and pipelined qdata staging of the line mapping, the point (3D) mapping, general and
-    even-odd contractions, 1 or 3 elements per block, both scatters: all within the parity tolerance."""
+    """Register, shared-memory, pipelined and bulk-copy qdata staging of the line mapping, the point (3D) mapping,
+    general and even-odd contractions, 1 or 3 elements per block, both scatters: all within the parity tolerance, and
+    no bounded wait gave up."""
     if staging == 3 and case.startswith("v"):
         pytest.skip("the pipelined kernel handles one component")
     for c in (ceed, ceed_det):
@@ -65,6 +66,7 @@ def test_every_kernel_variant(ceed, ceed_det, case, staging, epb, dtype):
         tol = 1e-12 if dtype == torch.float64 else 5e-5
         assert relinf(v.get_array_read(), g["v"]) < tol
         assert op.fused(lc.F64 if dtype == torch.float64 else lc.F32).tile()[2] == staging
+        assert c.status() == 0
 
 
 @pytest.mark.parametrize("case", ["poisson_n3_p4", "vpoisson_n4_p2", "mass_n8_p3", "kappa_n3_p3"])
