@@ -99,6 +99,18 @@ __device__ __forceinline__ dfloat mad(const dfloat &a, const dfloat &b, const df
   return df_fast_two_sum(s, t);
 }
 
+// Dot-product accumulator.  The generic form is a chain of fused multiply-adds; the float-float form follows Ogita,
+// Rump & Oishi's Dot2 ("Accurate sum and dot product", SIAM J. Sci. Comput. 2005): each product's error term (exact
+// FMA residual plus the cross terms) and each TwoSum error of the running high sum collect in one float, and the pair
+// is normalised once at the end (12 FP32 operations per term instead of 15 for a normalised multiply-add).
+template <typename T>
+struct Dot {
+  T                                 s;
+  __device__ __forceinline__ void   first(const T &a, const T &b) { s = a * b; }
+  __device__ __forceinline__ void   add(const T &a, const T &b) { s = mad(a, b, s); }
+  __device__ __forceinline__ T      value() const { return s; }
+};
+
 __device__ __forceinline__ dfloat operator*(const dfloat &a, const dfloat &b) {
   const float p = a.hi * b.hi;
   float       e = __fmaf_rn(a.hi, b.hi, -p);
@@ -114,6 +126,28 @@ __device__ __forceinline__ dfloat operator+(const dfloat &a, const dfloat &b) {
   t += a.lo + b.lo;
   return df_fast_two_sum(s, t);
 }
+
+template <>
+struct Dot<dfloat> {
+  float                             s, c;
+  __device__ __forceinline__ void   first(const dfloat &a, const dfloat &b) {
+    s = a.hi * b.hi;
+    c = __fmaf_rn(a.hi, b.hi, -s);
+    c = __fmaf_rn(a.hi, b.lo, c);
+    c = __fmaf_rn(a.lo, b.hi, c);
+  }
+  __device__ __forceinline__ void add(const dfloat &a, const dfloat &b) {
+    const float p  = a.hi * b.hi;
+    float       e  = __fmaf_rn(a.hi, b.hi, -p);
+    e              = __fmaf_rn(a.hi, b.lo, e);
+    e              = __fmaf_rn(a.lo, b.hi, e);
+    const float s2 = s + p;
+    const float bb = s2 - s;
+    c += ((s - (s2 - bb)) + (p - bb)) + e;
+    s = s2;
+  }
+  __device__ __forceinline__ dfloat value() const { return df_fast_two_sum(s, c); }
+};
 
 __device__ __forceinline__ dfloat operator-(const dfloat &a) {
   dfloat r;

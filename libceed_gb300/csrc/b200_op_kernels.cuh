@@ -169,10 +169,11 @@ template <typename T, int J, int K>
 __device__ __forceinline__ void mat_apply(const T *M, const T (&in)[K], T (&out)[J]) {
 #pragma unroll
   for (int j = 0; j < J; j++) {
-    T s = M[j * K] * in[0];
+    Dot<T> s;
+    s.first(M[j * K], in[0]);
 #pragma unroll
-    for (int k = 1; k < K; k++) s = mad(M[j * K + k], in[k], s);
-    out[j] = s;
+    for (int k = 1; k < K; k++) s.add(M[j * K + k], in[k]);
+    out[j] = s.value();
   }
 }
 
@@ -181,10 +182,11 @@ template <typename T, int J, int K>
 __device__ __forceinline__ void mat_apply_t(const T *M, const T (&in)[J], T (&out)[K]) {
 #pragma unroll
   for (int k = 0; k < K; k++) {
-    T s = M[k] * in[0];
+    Dot<T> s;
+    s.first(M[k], in[0]);
 #pragma unroll
-    for (int j = 1; j < J; j++) s = mad(M[j * K + k], in[j], s);
-    out[k] = s;
+    for (int j = 1; j < J; j++) s.add(M[j * K + k], in[j]);
+    out[k] = s.value();
   }
 }
 
@@ -201,29 +203,32 @@ __device__ __forceinline__ void eo_apply(const EOMat<T, J, K> &M, const T (&in)[
   }
 #pragma unroll
   for (int j = 0; j < Jh; j++) {
-    T e = M.E[j * Kh] * ie[0], o = M.O[j * Kh] * io[0];
+    Dot<T> de, dd;
+    de.first(M.E[j * Kh], ie[0]);
+    dd.first(M.O[j * Kh], io[0]);
 #pragma unroll
     for (int k = 1; k < Kh; k++) {
-      e = mad(M.E[j * Kh + k], ie[k], e);
-      o = mad(M.O[j * Kh + k], io[k], o);
+      de.add(M.E[j * Kh + k], ie[k]);
+      dd.add(M.O[j * Kh + k], io[k]);
     }
-    if constexpr (Km) e = mad(M.C[j], in[Kh], e);
+    if constexpr (Km) de.add(M.C[j], in[Kh]);
+    const T e = de.value(), o = dd.value();
     out[j]         = e + o;
     out[J - 1 - j] = PAR > 0 ? e - o : o - e;
   }
   if constexpr (Jm) {
+    Dot<T> r;
     if constexpr (PAR > 0) {
-      T r = M.R[0] * ie[0];
+      r.first(M.R[0], ie[0]);
 #pragma unroll
-      for (int k = 1; k < Kh; k++) r = mad(M.R[k], ie[k], r);
-      if constexpr (Km) r = mad(M.R[Kh], in[Kh], r);
-      out[Jh] = r;
+      for (int k = 1; k < Kh; k++) r.add(M.R[k], ie[k]);
+      if constexpr (Km) r.add(M.R[Kh], in[Kh]);
     } else {
-      T r = M.R[0] * io[0];
+      r.first(M.R[0], io[0]);
 #pragma unroll
-      for (int k = 1; k < Kh; k++) r = mad(M.R[k], io[k], r);
-      out[Jh] = r;
+      for (int k = 1; k < Kh; k++) r.add(M.R[k], io[k]);
     }
+    out[Jh] = r.value();
   }
 }
 

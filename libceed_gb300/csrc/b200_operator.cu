@@ -158,30 +158,37 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
 }
 
 // Default launch shape per precision and QFunction, from autotuner sweeps on GB300 (n^3 boxes of ~17M DoF, atomic
-// scatter).  Indexed by P_1d - 2; {staging, elements per block}.  The autotuner refines it per problem.
+// scatter, every staging and elements-per-block candidate).  Indexed by P_1d - 2; {staging, elements per block}.  The
+// autotuner refines it per problem.
 struct TileDefault {
   int stage, epb;
 };
-static const TileDefault kTileF64Grad[8]  = {{1, 14}, {4, 5}, {1, 5}, {4, 1}, {1, 5}, {1, 1}, {1, 2}, {2, 1}};
-static const TileDefault kTileF64Mass[8]  = {{1, 28}, {1, 8}, {1, 14}, {4, 1}, {1, 6}, {1, 2}, {1, 6}, {1, 2}};
-static const TileDefault kTileF32[8]      = {{1, 28}, {1, 6}, {1, 6}, {1, 6}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};
-static const TileDefault kTileF64XGrad[8] = {{1, 28}, {1, 10}, {1, 5}, {1, 7}, {1, 7}, {1, 1}, {2, 1}, {2, 1}};
-static const TileDefault kTileF64XMass[8] = {{1, 28}, {1, 8}, {1, 5}, {1, 5}, {1, 4}, {1, 4}, {1, 3}, {1, 2}};
+static const TileDefault kTileF64Grad[8]  = {{5, 14}, {4, 5}, {4, 1}, {4, 1}, {1, 5}, {5, 1}, {1, 2}, {5, 1}};
+static const TileDefault kTileF64Mass[8]  = {{5, 14}, {1, 8}, {4, 1}, {4, 1}, {1, 6}, {5, 1}, {1, 6}, {5, 2}};
+static const TileDefault kTileF32Grad[8]  = {{5, 14}, {5, 8}, {5, 5}, {5, 3}, {5, 1}, {5, 1}, {5, 1}, {5, 1}};
+static const TileDefault kTileF32Mass[8]  = {{1, 14}, {1, 4}, {1, 5}, {5, 7}, {1, 3}, {1, 3}, {5, 1}, {3, 1}};
+static const TileDefault kTileF64XGrad[8] = {{1, 7}, {1, 24}, {1, 10}, {5, 7}, {5, 4}, {1, 1}, {5, 2}, {5, 1}};
+static const TileDefault kTileF64XMass[8] = {{1, 7}, {1, 8}, {1, 5}, {1, 7}, {1, 5}, {1, 4}, {1, 3}, {1, 2}};
+static const TileDefault kTileVector[8]   = {{1, 14}, {1, 8}, {1, 7}, {1, 7}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};
 
 static void op_default_tile(b200_op op, int *epb, int *stage) {
-  const int Q = op->d.Q_1d, P = op->d.P_1d;
-  TileDefault t{kStageSmem, 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1};  // vector QFunctions
-  if (op->d.num_comp == 1 && P >= kOpPMin && P <= kOpPMax) {
+  const int   Q = op->d.Q_1d, P = op->d.P_1d;
+  TileDefault t{kStageReg, 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1};
+  if (P >= kOpPMin && P <= kOpPMax) {
     const bool mass = op->d.qf == B200_QF_MASS;
-    if (op->d.prec == B200_F64) t = (mass ? kTileF64Mass : kTileF64Grad)[P - 2];
+    if (op->d.num_comp > 1) t = kTileVector[P - 2];
+    else if (op->d.prec == B200_F64) t = (mass ? kTileF64Mass : kTileF64Grad)[P - 2];
     else if (op->d.prec == B200_F64X) t = (mass ? kTileF64XMass : kTileF64XGrad)[P - 2];
-    else t = kTileF32[P - 2];
+    else t = (mass ? kTileF32Mass : kTileF32Grad)[P - 2];
   }
+  // The pipelined kernel needs a centro-symmetric basis: without one the default falls back to register staging.
+  if (t.stage == kStagePipe && !op->symmetric) t = {kStageReg, t.epb};
   if (*stage <= 0) *stage = t.stage;
   if (*epb <= 0) {
-    *epb = *stage == t.stage ? t.epb : (256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1);
-    if (*stage == kStagePipe) *epb = 128 / (Q * Q) > 0 ? 128 / (Q * Q) : 1;
-    if (*stage == kStage3D) *epb = 512 / (Q * Q * Q) > 0 ? 512 / (Q * Q * Q) : 1;
+    if (*stage == t.stage) *epb = t.epb;
+    else if (*stage == kStagePipe) *epb = 128 / (Q * Q) > 0 ? 128 / (Q * Q) : 1;
+    else if (*stage == kStage3D) *epb = 512 / (Q * Q * Q) > 0 ? 512 / (Q * Q * Q) : 1;
+    else *epb = 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1;
   }
 }
 

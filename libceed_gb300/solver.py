@@ -17,7 +17,7 @@ def cg_solve(ceed, op, qdata64, mask, b, x, mixed=False, op32=None, qdata32=None
     o = CGOpts(rtol, max_it, 1 if mixed else 0, inner_rtol, max_outer, 1 if use_graph else 0, check_every,
                jacobi.data.data_ptr() if jacobi is not None else None)
     s = CGStats()
-    f64 = op.fused(F64)
+    f64 = op.fused(op._kernel_prec(F64))  # F64X kernels when op.arithmetic == "float-float" (same double vectors)
     f32 = op32.fused(F32).h if mixed else None
     call("b200_cg_solve", ceed._ctx, f64.h, f32, qdata64.ptr(), qdata32.ptr() if mixed else None, mask.ptr(), b.ptr(), x.ptr(),
          b.size, ctypes.byref(o), ctypes.byref(s))

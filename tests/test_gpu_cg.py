@@ -48,6 +48,23 @@ def test_cg_reaches_tolerance(problem, mixed, graph):
     assert np.linalg.norm(r) / np.linalg.norm(bh) < 2e-10
 
 
+def test_float_float_cg_matches_fp64(problem):
+    """CG on the float-float operator (FP64 vectors and Krylov arithmetic, F64X apply) reaches the FP64 tolerance and
+    the oracle-checked residual, in about the FP64 iteration count."""
+    ceed, box, o64, o32, mask, b, m, bh, pb = problem
+    x64, xff = ceed.Vector(box.l_size), ceed.Vector(box.l_size)
+    s64 = cg_solve(ceed, o64["op"], o64["qdata"], mask, b, x64, rtol=1e-10, check_every=10)
+    o64["op"].arithmetic = "float-float"
+    try:
+        sff = cg_solve(ceed, o64["op"], o64["qdata"], mask, b, xff, rtol=1e-10, check_every=10)
+    finally:
+        o64["op"].arithmetic = "native"
+    assert sff["converged"] and sff["rel_residual"] <= 1e-10
+    assert abs(sff["iterations"] - s64["iterations"]) <= max(3, s64["iterations"] // 20)
+    r = m * (bh - pb.apply(m * xff.get_array_read()))
+    assert np.linalg.norm(r) / np.linalg.norm(bh) < 2e-10
+
+
 def test_graph_and_eager_agree(problem):
     """With the deterministic scatter, graph-captured and eager solves run the same kernels in the same order."""
     _, box, _, _, _, _, m, bh, _ = problem
