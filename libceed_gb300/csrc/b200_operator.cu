@@ -233,7 +233,7 @@ extern "C" int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *o
   B200_CHECK(d.P_1d >= kOpPMin && d.P_1d <= kOpPMax, B200_ERROR_UNSUPPORTED, "fused kernels cover P_1d in %d..%d (got %d)", kOpPMin, kOpPMax, d.P_1d);
   const int nc_expected = (d.qf == B200_QF_VECMASS || d.qf == B200_QF_VECPOISSON) ? 3 : 1;
   B200_CHECK(d.num_comp == nc_expected, B200_ERROR_DIMENSION, "QFunction %d needs %d components (got %d)", d.qf, nc_expected, d.num_comp);
-  B200_CHECK(d.offsets && d.interp_1d && d.grad_1d, B200_ERROR_INCOMPLETE, "b200_op_create: offsets and 1D matrices are required");
+  B200_CHECK((d.offsets || d.num_elem == 0) && d.interp_1d && d.grad_1d, B200_ERROR_INCOMPLETE, "b200_op_create: offsets and 1D matrices are required");
   B200_CHECK(d.scatter == B200_SCATTER_ATOMIC || d.scatter == B200_SCATTER_DETERMINISTIC, B200_ERROR_UNSUPPORTED, "unknown scatter mode %d",
              d.scatter);
   B200_CHECK(d.num_elem >= 0 && d.num_elem <= (int64_t)INT32_MAX * 64, B200_ERROR_DIMENSION, "num_elem %lld out of range", (long long)d.num_elem);
@@ -283,13 +283,14 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   b200_ctx            ctx = op->ctx;
   const b200_op_desc &d   = op->d;
   B200_CHECK(!op->jit, B200_ERROR_INCOMPATIBLE, "operator has a run-time compiled QFunction: use b200_op_apply_jit");
-  B200_CHECK(u && v && qdata, B200_ERROR_INCOMPLETE, "b200_op_apply: u, v and qdata are required");
-  B200_CHECK(d.qf != B200_QF_POISSON_KAPPA || kappa, B200_ERROR_INCOMPLETE, "kappa-weighted diffusion needs kappa");
+  B200_CHECK(v || d.l_size == 0, B200_ERROR_INCOMPLETE, "b200_op_apply: v is required");
   const size_t tsz = storage_bytes(d.prec);
-  if (d.num_elem == 0) {
-    if (!add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
+  if (d.num_elem == 0) {  // no elements: Apply zeroes v, ApplyAdd leaves it
+    if (!add && d.l_size > 0) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
     return B200_SUCCESS;
   }
+  B200_CHECK(u && qdata, B200_ERROR_INCOMPLETE, "b200_op_apply: u and qdata are required");
+  B200_CHECK(d.qf != B200_QF_POISSON_KAPPA || kappa, B200_ERROR_INCOMPLETE, "kappa-weighted diffusion needs kappa");
   OpLaunch r{};
   r.num_elem    = d.num_elem;
   r.comp_stride = d.comp_stride;
@@ -393,7 +394,7 @@ static int op_common_init(b200_ctx ctx, const b200_op_desc &d, b200_op op) {
   B200_CHECK(d.prec == B200_F64 || d.prec == B200_F32, B200_ERROR_UNSUPPORTED, "unknown precision %d", d.prec);
   B200_CHECK(d.Q_1d == d.P_1d + 1, B200_ERROR_UNSUPPORTED, "fused kernels are compiled for Q_1d = P_1d + 1 (got P=%d, Q=%d)", d.P_1d, d.Q_1d);
   B200_CHECK(d.P_1d >= kOpPMin && d.P_1d <= kOpPMax, B200_ERROR_UNSUPPORTED, "fused kernels cover P_1d in %d..%d (got %d)", kOpPMin, kOpPMax, d.P_1d);
-  B200_CHECK(d.offsets && d.interp_1d && d.grad_1d, B200_ERROR_INCOMPLETE, "offsets and 1D matrices are required");
+  B200_CHECK((d.offsets || d.num_elem == 0) && d.interp_1d && d.grad_1d, B200_ERROR_INCOMPLETE, "offsets and 1D matrices are required");
   B200_CHECK(d.scatter == B200_SCATTER_ATOMIC || d.scatter == B200_SCATTER_DETERMINISTIC, B200_ERROR_UNSUPPORTED, "unknown scatter mode %d",
              d.scatter);
   op->ctx    = ctx;

@@ -37,13 +37,17 @@ def build_poisson(ceed, box, dtype=torch.float64, qf_name=None):
     return dict(op=op, qdata=qdata, ru=ru, rq=rq, bu=bu, build=build, X=X)
 
 
-def run_poisson(n=3, degree=3, device="cuda:0", seed=11):
-    """Apply the FP64 Poisson operator to the seeded input; returns v on the host."""
+def run_poisson(n=3, degree=3, device="cuda:0", seed=11, family="f64"):
+    """Apply the Poisson operator to the seeded input; returns v on the host.  family: "f64" (FP64 kernels), "f64x"
+    (float-float kernels on the same double vectors) or "f32" (FP32 vectors and kernels)."""
     ceed = Ceed("/gpu/cuda/b200:device_id=" + str(torch.device(device).index or 0))
     box = mesh.Box(n, degree, noise=0.05, seed=seed)
-    objs = build_poisson(ceed, box)
-    u = ceed.Vector(box.l_size)
+    dt = torch.float32 if family == "f32" else torch.float64
+    objs = build_poisson(ceed, box, dtype=dt)
+    if family == "f64x":
+        objs["op"].arithmetic = "float-float"
+    u = ceed.Vector(box.l_size, dt)
     u.set_array(box.u())
-    v = ceed.Vector(box.l_size)
+    v = ceed.Vector(box.l_size, dt)
     objs["op"].apply(u, v)
-    return v.get_array_read()
+    return v.get_array_read().astype("float64")

@@ -90,3 +90,53 @@ def apply_cached(op, prec=F64):
         op.elems_per_block = entry["epb"]
         op.staging = STAGE_CODES[entry["staging"]]
     return entry
+
+
+# Box sizes of the per-degree workload (~16-18 M DoF for scalar fields).
+BOX_N = {1: 256, 2: 128, 3: 85, 4: 64, 5: 52, 6: 43, 7: 37, 8: 32}
+
+
+def sweep_main(argv=None):
+    """Tile sweep of the scalar Poisson and mass operators over degrees and kernel families; one JSON line per
+    (degree, QFunction, family) with the best tile and the best rate of every staging.  Needs a GPU.
+
+        python -m libceed_gb300.tune --degrees 1,2,3,4,5,6,7,8
+    """
+    import argparse
+
+    import torch
+
+    from . import mesh
+    from .ceed import Ceed
+    from .smoke_case import build_poisson
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--degrees", default="1,2,3,4,5,6,7,8")
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args(argv)
+    ceed = Ceed("/gpu/cuda/b200")
+    for p in [int(x) for x in a.degrees.split(",")]:
+        box = mesh.Box(BOX_N[p], p, noise=0.05, seed=5)
+        for qf in ("Poisson3DApply", "MassApply"):
+            for tag, dt, arith in (("f64", torch.float64, "native"), ("f32", torch.float32, "native"), ("f64x", torch.float64, "float-float")):
+                objs = build_poisson(ceed, box, dtype=dt, qf_name=qf)
+                op = objs["op"]
+                op.arithmetic = arith
+                u = ceed.Vector(box.l_size, dt)
+                u.set_array(box.u())
+                v = ceed.Vector(box.l_size, dt)
+                r = autotune(op, u, v, reps=a.reps, use_cache=False)
+                by = {}
+                for x in r["sweep"]:
+                    if x["staging"] not in by or x["ms"] < by[x["staging"]]["ms"]:
+                        by[x["staging"]] = x
+                print(json.dumps(dict(degree=p, qfunction=qf, family=tag, dof=box.l_size,
+                                      best=dict(epb=r["epb"], staging=r["staging"], gdofs=round(box.l_size / r["ms"] / 1e6, 3)),
+                                      per_staging={k: [x["epb"], round(box.l_size / x["ms"] / 1e6, 3)] for k, x in by.items()},
+                                      status=ceed.status())), flush=True)
+                del objs, op, u, v
+                torch.cuda.empty_cache()
+
+
+if __name__ == "__main__":
+    sweep_main()

@@ -1,0 +1,70 @@
+"""Edge cases of the fused apply: ragged last element batches for every staging, elements-per-block and kernel
+family (against the reference's golden vectors), and operators with no elements (Apply zeroes the output,
+ApplyAdd leaves it), as the reference's restriction and operator tests cover empty and partial blocks."""
+import numpy as np
+import pytest
+import torch
+
+import libceed_gb300 as lc
+from tests.conftest import relinf
+from tests.gpu_cases import setup
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ceed():
+    return lc.Ceed("/gpu/cuda/b200")
+
+
+@pytest.fixture(scope="module")
+def ceed_det():
+    return lc.Ceed("/gpu/cuda/b200", deterministic=True)
+
+
+@pytest.mark.parametrize("case", ["poisson_n3_p4", "mass_n8_p3"])
+@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("epb", [2, 4, 5, 7])
+@pytest.mark.parametrize("family", ["f64", "f32", "f64x"])
+def test_ragged_last_block(ceed, ceed_det, case, staging, epb, family):
+    """27 or 512 elements in batches of 2, 4, 5 or 7: the last batch is partial."""
+    if family == "f64x" and staging in (3, 4):
+        pytest.skip("float-float kernels: register, shared and bulk-copy staging")
+    dt = torch.float32 if family == "f32" else torch.float64
+    for c in (ceed, ceed_det):
+        kind, box, g, objs = setup(c, case, dtype=dt)
+        op = objs["op"]
+        op.elems_per_block, op.staging = epb, staging
+        if family == "f64x":
+            op.arithmetic = "float-float"
+        u = c.Vector(box.l_size, dt)
+        u.set_array(box.u())
+        v = c.Vector(box.l_size, dt)
+        v.set_value(7.0)
+        op.apply(u, v)
+        assert relinf(v.get_array_read(), g["v"]) < (5e-5 if family == "f32" else 1e-12)
+        assert c.status() == 0
+
+
+@pytest.mark.parametrize("qf", ["Poisson3DApply", "MassApply"])
+@pytest.mark.parametrize("det", [False, True])
+def test_operator_without_elements(ceed, ceed_det, qf, det):
+    c = ceed_det if det else ceed
+    P, Q, n = 5, 6, 10
+    poisson = qf.startswith("Poisson")
+    ru = c.ElemRestriction(0, P ** 3, 1, 1, n, np.zeros(0, np.int32))
+    rq = c.StridedElemRestriction(0, Q ** 3, 6 if poisson else 1, 0, lc.STRIDES_BACKEND)
+    bu = c.BasisTensorH1Lagrange(3, 1, P, Q, lc.GAUSS)
+    op = c.Operator(c.QFunctionByName(qf))
+    fin, fout = ("du", "dv") if poisson else ("u", "v")
+    op.set_field(fin, ru, bu, "active")
+    op.set_field("qdata", rq, None, c.Vector(0))
+    op.set_field(fout, ru, bu, "active")
+    u, v = c.Vector(n), c.Vector(n)
+    u.set_value(1.0)
+    v.set_value(3.0)
+    op.apply(u, v)
+    assert np.all(v.get_array_read() == 0.0)
+    v.set_value(3.0)
+    op.apply_add(u, v)
+    assert np.all(v.get_array_read() == 3.0)
