@@ -17,6 +17,7 @@
 typedef struct {
   b200_ctx ctx;
   int      device_id;
+  bool     float_float;  // resource option ":arithmetic=float-float"
 } Ceed_B200;
 
 // Host and device mirrors of a CeedVector (the copy-mode rules of backends/cuda/ceed-cuda-common.c:53-80).

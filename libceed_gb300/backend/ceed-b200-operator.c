@@ -256,7 +256,17 @@ static int OperatorAnalyse_B200(CeedOperator op) {
       d.interp_1d   = interp;
       d.grad_1d     = grad;
     }
-    CeedCallB200(ceed, b200_op_create(ctx, &d, &impl->op));
+    {
+      Ceed_B200 *data;
+
+      CeedCallBackend(CeedGetData(ceed, &data));
+      // Float-float arithmetic where its kernels exist (scalar mass and Poisson, centro-symmetric bases); FP64 else.
+      if (data->float_float && (d.qf == B200_QF_MASS || d.qf == B200_QF_POISSON)) {
+        d.prec = B200_F64X;
+        if (b200_op_create(ctx, &d, &impl->op)) d.prec = B200_F64;
+      }
+    }
+    if (d.prec == B200_F64) CeedCallB200(ceed, b200_op_create(ctx, &d, &impl->op));
     impl->qdata   = vq;  // reference kept until destroy
     impl->kind    = 1;
     impl->qf_kind = qf_impl->qf_kind;

@@ -2,6 +2,7 @@
 // and on `/cpu/self/ref/serial` in one process and the applies compared (relative l-infinity, tolerance 1e-12):
 //   1. gallery Poisson3DBuild + Poisson3DApply on a perturbed box of hexahedra (fused compiled kernel);
 //      and its assembled diagonal (CeedOperatorLinearAssembleDiagonal);
+//      the same with the resource option ":arithmetic=float-float" (float-float kernels on double vectors);
 //   2. gallery Mass3DBuild + the user QFunction ScaledMass from tests/qfunctions/user-qfunctions.h with a context
 //      (NVRTC-compiled on /gpu/cuda/b200, the function pointer on the CPU backend).
 // Needs a GPU and a libCEED build; prints nothing on success, like the reference's tests/t*.c.
@@ -179,6 +180,11 @@ int main(void) {
   err = 0, scale = 0;
   for (int i = 0; i < N; i++) err = fmax(err, fabs(d_gpu[i] - d_ref[i])), scale = fmax(scale, fabs(d_ref[i]));
   if (err > 1e-12 * scale) printf("Error: assembled diagonal on /gpu/cuda/b200 differs by %e (relative)\n", err / scale);
+  fail |= err > 1e-12 * scale;
+  Apply("/gpu/cuda/b200:arithmetic=float-float", n, P, coords, xoff, uoff, u, v_gpu, d_gpu);
+  err = 0, scale = 0;
+  for (int i = 0; i < N; i++) err = fmax(err, fabs(v_gpu[i] - v_ref[i])), scale = fmax(scale, fabs(v_ref[i]));
+  if (err > 1e-12 * scale) printf("Error: float-float apply on /gpu/cuda/b200 differs by %e (relative)\n", err / scale);
   fail |= err > 1e-12 * scale;
   free(d_gpu), free(d_ref);
   ApplyUserMass("/gpu/cuda/b200", n, P, coords, xoff, uoff, u, v_gpu);
