@@ -145,6 +145,23 @@ def ncu_traffic(key):
         return None
 
 
+def max_over_ranks(values, world, device="cpu"):
+    """Element-wise maximum over all ranks of per-rank timings (the job's time is its slowest replica's)."""
+    import torch
+
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_rate(dof_per_rank, world, steps, ms_max):
+    """Whole-job GDoF/s of N independent replicas: all ranks' DoF over the slowest rank's time."""
+    return dof_per_rank * world * steps / (ms_max * 1e-3) / 1e9
+
+
 # ------------------------------------------------------------------------------------------------------------------
 # GPU side
 # ------------------------------------------------------------------------------------------------------------------
@@ -244,10 +261,7 @@ def gpu_main(a, rank, world, local_rank):
     barrier()
     e2e_ms = x0.elapsed_time(x1)
 
-    t = torch.tensor([ms_total, e2e_ms, kernel_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_total, e2e_ms, kernel_ms = t.tolist()
+    ms_total, e2e_ms, kernel_ms = max_over_ranks([ms_total, e2e_ms, kernel_ms], world, "cuda")
 
     extras = {}
     if rank == 0 and not a.no_extras:
@@ -255,8 +269,7 @@ def gpu_main(a, rank, world, local_rank):
 
     if rank != 0:
         return None
-    dof_total = box.l_size * world * a.steps
-    value = dof_total / (ms_total * 1e-3) / 1e9
+    value = replica_rate(box.l_size, world, a.steps, ms_total)
     bytes_alg, flops_alg = fused.cost()
     peaks, peak_kind = measured_peaks()
     achieved = bytes_alg / (kernel_ms * 1e-3) / 1e9
@@ -281,7 +294,7 @@ def gpu_main(a, rank, world, local_rank):
                    "degree": degree, "elements": box.num_elem, "dof": box.l_size, "scatter": "atomic",
                    "l2": "inputs larger than L2 (qdata %.2f GB)" % (6 * 8 * box.num_elem * box.Q ** 3 / 1e9),
                    "parallelism": f"replicas x{world}", "tile": {"elems_per_block": epb, "threads_per_block": tpb, "staging": staging}},
-        "e2e": {"value": round(box.l_size * world * a.steps / (e2e_ms * 1e-3) / 1e9, 4), "unit": "GDoF/s",
+        "e2e": {"value": round(replica_rate(box.l_size, world, a.steps, e2e_ms), 4), "unit": "GDoF/s",
                 "h2d_bytes_per_step": 8 * box.l_size, "d2h_bytes_per_step": 8 * box.l_size,
                 "pipeline": "pinned H2D, apply, D2H on three streams, double-buffered (copies of neighbouring steps overlap the apply)"},
         "gpu_launches": int(launches),
@@ -442,7 +455,7 @@ def reference_main(a, rank, world):
     # K steps, each a bounded sample of the workload on all host cores.
     vals = []
     for _ in range(a.warmup):
-        pass
+        cpu_reference_rate(a.degree, seconds_target=0.3, cores=cores)
     t0 = time.perf_counter()
     for _ in range(a.steps):
         r, _, _ = cpu_reference_rate(a.degree, seconds_target=1.0, cores=cores)
