@@ -168,7 +168,8 @@ typedef struct {
 
 int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);
 /* v = A u (add = 0, CeedOperatorApply) or v += A u (add = 1, CeedOperatorApplyAdd).  qdata: [comp][elem][qpt] in
- * the operator's precision; kappa: [elem][qpt] or NULL. */
+ * the operator's storage precision (double for B200_F64 and B200_F64X); kappa: [elem][qpt] or NULL.  With no elements
+ * Apply zeroes v and ApplyAdd leaves it; u and qdata may then be NULL. */
 int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add);
 /* Algorithmic bytes and FLOPs of one apply (for roofline reporting). */
 int b200_op_cost(b200_op op, double *bytes, double *flops);
@@ -178,7 +179,9 @@ int b200_op_set_tile(b200_op op, int elems_per_block, int staging);
 /* Largest elements-per-block the kernel of a staging mode can launch with (threads and shared memory). */
 int b200_op_tile_limits(b200_op op, int staging, int *max_elems_per_block);
 /* Device time of one v += A u with the current tile, averaged over reps launches (CUDA events; used by the
- * autotuner, which sweeps elements per block and qdata staging per (P, Q, components, precision)). */
+ * autotuner, which sweeps elements per block, thread mapping and qdata staging per (P, Q, components, precision)).
+ * No counterpart in the reference, whose cuda-gen backend sizes blocks by a heuristic
+ * (backends/cuda-gen/ceed-cuda-gen-operator.c:40-97). */
 int b200_op_time(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int reps, double *ms_per_apply);
 int b200_op_destroy(b200_op op);
 

@@ -496,18 +496,25 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     }
   };
 
+  // Thread (a, b), a, b < P, gathers and later scatters the element's x-line of nodes (p, a, b): its P offsets stay
+  // in registers from the gather to the scatter.
+  const bool owner = a < P && b < P;
+  int32_t    off_line[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) off_line[p] = (owner && active) ? args.offsets[e * P3 + P * (a + P * b) + p] : 0;
+
 #pragma unroll 1
   for (int c = 0; c < NC; c++) {
     if (c > 0) __syncthreads();
-    for (int i = tid; i < P3; i += Q2) {
-      const int x = i % P, y = (i / P) % P, z = i / (P * P);
-      s0[B200_IDX(x, y, z)] = active ? T(args.u[(int64_t)args.offsets[e * P3 + i] + c * args.comp_stride]) : T(0);
+    if (owner) {
+#pragma unroll
+      for (int p = 0; p < P; p++) s0[B200_IDX(p, a, b)] = active ? T(args.u[(int64_t)off_line[p] + c * args.comp_stride]) : T(0);
     }
     __syncthreads();
     T out[P];
     if (c == 0) op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out, qwait);
     else op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out);
-    if (a < P && b < P && active) scatter_line<T, P>(args, e, c, args.offsets + e * P3 + P * (a + P * b), a, b, out);
+    if (owner && active) scatter_line<T, P>(args, e, c, off_line, a, b, out);
   }
 }
 
