@@ -224,7 +224,7 @@ int b200_op_apply_jit(b200_op op, const void *u, void *v, const void *const *pas
 int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qdata, void *g);
 
 /* ---- Conjugate gradients on the fused operator (no libCEED counterpart: the reference solves with PETSc KSPCG around
- *      CeedOperatorApply in examples/petsc/bps.c).  Homogeneous Dirichlet conditions through mask (1 free, 0 fixed):
+ *      CeedOperatorApply in examples/petsc/bps.c).  Homogeneous Dirichlet conditions through mask (exactly 1 free, 0 fixed):
  *      solves m A(m x) = m b from x = 0.  mixed = 0: FP64 CG.  mixed = 1: FP32 CG (op32, qdata32) on the defect
  *      r = m(b - A64 x), computed in FP64, until |r| / |b| <= rtol.  Dot products and norms accumulate in FP64.
  *      Blocks of check_every iterations run as one CUDA graph when use_graph = 1.  b, x, mask: FP64 device arrays

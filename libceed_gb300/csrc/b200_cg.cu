@@ -19,28 +19,67 @@ namespace b200 {
 // (z = M r with the Jacobi preconditioner M = diag(A)^-1, or z = r without one, when [2] is r.r itself).
 enum { kRR = 0, kPW = 1, kRRNew = 2, kRes = 3 };
 
+// The reduction kernels run on a fixed grid of two blocks per SM (so that their sums are reproducible), which leaves
+// few threads to keep HBM busy: each thread therefore loads kUnroll<T> elements (at i, i + stride, ...) before using
+// any of them.  Partial sums are still accumulated in index order i, i + stride, ..., as a plain loop would.
 template <typename T>
-__global__ void __launch_bounds__(kReduceThreads) k_cg_mask_dot(int64_t n, const T *__restrict__ mask, const T *__restrict__ p, T *__restrict__ w,
-                                                                  double *__restrict__ partial) {
-  double acc = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const T wi = w[i] * mask[i];
-    w[i]       = wi;
-    acc += (double)p[i] * (double)wi;
+constexpr int kUnroll = sizeof(T) == 4 ? 16 : 8;
+
+// p.w (the operator output w unmasked: p is zero on the Dirichlet nodes, so p.w = p.(m w) term by term).
+template <typename T>
+__global__ void __launch_bounds__(kReduceThreads) k_cg_pdot(int64_t n, const T *__restrict__ p, const T *__restrict__ w, double *__restrict__ partial) {
+  constexpr int U      = kUnroll<T>;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double        acc    = 0.0;
+  for (; i + (U - 1) * stride < n; i += U * stride) {
+    T wv[U], pv[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      wv[k] = w[i + k * stride];
+      pv[k] = p[i + k * stride];
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) acc += (double)pv[k] * (double)wv[k];
   }
+  for (; i < n; i += stride) acc += (double)p[i] * (double)w[i];
   acc = block_reduce(kRedDot, acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
+// x += alpha p, r = m (r - alpha w), and the partial sums of r.r.  The mask (0 or 1) applied here is the m of m A(m x):
+// r stays zero on the Dirichlet nodes.
 template <typename T>
-__global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const double *__restrict__ s, T *__restrict__ x, T *__restrict__ r,
-                                                                const T *__restrict__ p, const T *__restrict__ w, double *__restrict__ partial) {
-  const double pw    = s[kPW];
-  const T      alpha = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
-  double       acc   = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const double *__restrict__ s, const T *__restrict__ mask, T *__restrict__ x,
+                                                                T *__restrict__ r, const T *__restrict__ p, const T *__restrict__ w,
+                                                                double *__restrict__ partial) {
+  constexpr int U      = kUnroll<T>;
+  const double  pw     = s[kPW];
+  const T       alpha  = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double        acc    = 0.0;
+  for (; i + (U - 1) * stride < n; i += U * stride) {
+    T xv[U], pv[U], rv[U], wv[U], mv[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      xv[k] = x[i + k * stride];
+      pv[k] = p[i + k * stride];
+      rv[k] = r[i + k * stride];
+      wv[k] = w[i + k * stride];
+      mv[k] = mask[i + k * stride];
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      x[i + k * stride] = xv[k] + alpha * pv[k];
+      const T ri        = mv[k] * (rv[k] - alpha * wv[k]);
+      r[i + k * stride] = ri;
+      acc += (double)ri * (double)ri;
+    }
+  }
+  for (; i < n; i += stride) {
     x[i] += alpha * p[i];
-    const T ri = r[i] - alpha * w[i];
+    const T ri = mask[i] * (r[i] - alpha * w[i]);
     r[i]       = ri;
     acc += (double)ri * (double)ri;
   }
@@ -50,15 +89,41 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const d
 
 // Preconditioned update: also z = M r, with partial sums of r.z (partial) and r.r (partial2).
 template <typename T>
-__global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const double *__restrict__ s, T *__restrict__ x, T *__restrict__ r,
-                                                                 T *__restrict__ z, const T *__restrict__ inv_diag, const T *__restrict__ p,
-                                                                 const T *__restrict__ w, double *__restrict__ partial, double *__restrict__ partial2) {
-  const double pw    = s[kPW];
-  const T      alpha = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
-  double       rz = 0.0, rr = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const double *__restrict__ s, const T *__restrict__ mask, T *__restrict__ x,
+                                                                 T *__restrict__ r, T *__restrict__ z, const T *__restrict__ inv_diag,
+                                                                 const T *__restrict__ p, const T *__restrict__ w, double *__restrict__ partial,
+                                                                 double *__restrict__ partial2) {
+  constexpr int U      = kUnroll<T>;
+  const double  pw     = s[kPW];
+  const T       alpha  = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double        rz = 0.0, rr = 0.0;
+  for (; i + (U - 1) * stride < n; i += U * stride) {
+    T xv[U], pv[U], rv[U], wv[U], dv[U], mv[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      xv[k] = x[i + k * stride];
+      pv[k] = p[i + k * stride];
+      rv[k] = r[i + k * stride];
+      wv[k] = w[i + k * stride];
+      dv[k] = inv_diag[i + k * stride];
+      mv[k] = mask[i + k * stride];
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      x[i + k * stride] = xv[k] + alpha * pv[k];
+      const T ri        = mv[k] * (rv[k] - alpha * wv[k]);
+      const T zi        = dv[k] * ri;
+      r[i + k * stride] = ri;
+      z[i + k * stride] = zi;
+      rz += (double)ri * (double)zi;
+      rr += (double)ri * (double)ri;
+    }
+  }
+  for (; i < n; i += stride) {
     x[i] += alpha * p[i];
-    const T ri = r[i] - alpha * w[i];
+    const T ri = mask[i] * (r[i] - alpha * w[i]);
     const T zi = inv_diag[i] * ri;
     r[i]       = ri;
     z[i]       = zi;
@@ -77,9 +142,22 @@ __global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const 
 // p = src + beta p, src = r (plain CG) or z (preconditioned).
 template <typename T>
 __global__ void k_cg_direction(int64_t n, const double *__restrict__ s, const T *__restrict__ src, T *__restrict__ p) {
-  const double rr   = s[kRR];
-  const T      beta = (T)(rr != 0.0 ? s[kRRNew] / rr : 0.0);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = src[i] + beta * p[i];
+  constexpr int U      = 4;
+  const double  rr     = s[kRR];
+  const T       beta   = (T)(rr != 0.0 ? s[kRRNew] / rr : 0.0);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + (U - 1) * stride < n; i += U * stride) {
+    T sv[U], pv[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      sv[k] = src[i + k * stride];
+      pv[k] = p[i + k * stride];
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) p[i + k * stride] = sv[k] + beta * pv[k];
+  }
+  for (; i < n; i += stride) p[i] = src[i] + beta * p[i];
 }
 
 // Start of a preconditioned solve: z = p = M r.
@@ -107,8 +185,25 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_final(int blocks, const d
 // r = m (b - r) and its squared norm (r holds A x on entry).
 __global__ void __launch_bounds__(kReduceThreads) k_residual(int64_t n, const double *__restrict__ mask, const double *__restrict__ b,
                                                                double *__restrict__ r, double *__restrict__ partial) {
-  double acc = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double        acc    = 0.0;
+  for (; i + (kUnroll<double> - 1) * stride < n; i += kUnroll<double> * stride) {
+    double mv[kUnroll<double>], bv[kUnroll<double>], rv[kUnroll<double>];
+#pragma unroll
+    for (int k = 0; k < kUnroll<double>; k++) {
+      mv[k] = mask[i + k * stride];
+      bv[k] = b[i + k * stride];
+      rv[k] = r[i + k * stride];
+    }
+#pragma unroll
+    for (int k = 0; k < kUnroll<double>; k++) {
+      const double ri   = mv[k] * (bv[k] - rv[k]);
+      r[i + k * stride] = ri;
+      acc += ri * ri;
+    }
+  }
+  for (; i < n; i += stride) {
     const double ri = mask[i] * (b[i] - r[i]);
     r[i]            = ri;
     acc += ri * ri;
@@ -160,17 +255,17 @@ static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mas
   for (int it = 0; it < count; it++) {
     int st = b200_op_apply(op, p, w, qdata, nullptr, 0);
     if (st) return st;
-    k_cg_mask_dot<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, mask, p, w, wk.partial);
-    B200_LAUNCHED(ctx, "cg_mask_dot");
+    k_cg_pdot<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, p, w, wk.partial);
+    B200_LAUNCHED(ctx, "cg_pdot");
     k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kPW, 1);
     B200_LAUNCHED(ctx, "cg_final");
     if (inv) {
-      k_pcg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, x, r, z, inv, p, w, wk.partial, wk.partial2);
+      k_pcg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, mask, x, r, z, inv, p, w, wk.partial, wk.partial2);
       B200_LAUNCHED(ctx, "pcg_update");
       k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial2, wk.s, kRes, 0);
       B200_LAUNCHED(ctx, "cg_final");
     } else {
-      k_cg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, x, r, p, w, wk.partial);
+      k_cg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, mask, x, r, p, w, wk.partial);
       B200_LAUNCHED(ctx, "cg_update");
     }
     k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kRRNew, 0);

@@ -30,19 +30,35 @@ __device__ __forceinline__ double block_reduce(int kind, double v) {
   return v;
 }
 
+__device__ __forceinline__ double red_term(int kind, double acc, double xi, double yi) {
+  switch (kind) {
+    case kRedSumSq: return acc + xi * xi;
+    case kRedAbsSum: return acc + fabs(xi);
+    case kRedMaxAbs: return fmax(acc, fabs(xi));
+    default: return acc + xi * yi;
+  }
+}
+
+// The fixed grid leaves few threads per SM, so each thread loads 8 elements (i, i + stride, ...) before combining
+// them; the combination order is the plain loop's, so the result does not depend on the unrolling.
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) k_reduce_partial(int kind, int64_t n, const T *__restrict__ x, const T *__restrict__ y,
                                                                    double *__restrict__ partial) {
-  double acc = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double xi = (double)x[i];
-    switch (kind) {
-      case kRedSumSq: acc += xi * xi; break;
-      case kRedAbsSum: acc += fabs(xi); break;
-      case kRedMaxAbs: acc = fmax(acc, fabs(xi)); break;
-      default: acc += xi * (double)y[i]; break;
+  constexpr int U      = 8;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double        acc    = 0.0;
+  for (; i + (U - 1) * stride < n; i += U * stride) {
+    T xv[U], yv[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      xv[k] = x[i + k * stride];
+      yv[k] = kind == kRedDot ? y[i + k * stride] : T(0);
     }
+#pragma unroll
+    for (int k = 0; k < U; k++) acc = red_term(kind, acc, (double)xv[k], (double)yv[k]);
   }
+  for (; i < n; i += stride) acc = red_term(kind, acc, (double)x[i], kind == kRedDot ? (double)y[i] : 0.0);
   acc = block_reduce(kind, acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }

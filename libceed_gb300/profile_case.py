@@ -27,7 +27,10 @@ def main():
     ap.add_argument("--ncomp", type=int, default=1)
     ap.add_argument("--epb", type=int, default=0)
     ap.add_argument("--staging", type=int, default=0)
+    ap.add_argument("--cg", action="store_true", help="time the FP64 and FP32-refined CG solves of the box instead")
     a = ap.parse_args()
+    if a.cg:
+        return cg_case(a)
     dt = torch.float32 if a.prec == "f32" else torch.float64
     ceed = lc.Ceed("/gpu/cuda/b200", deterministic=a.det)
     box = mesh.Box(a.n, a.degree, ncomp=a.ncomp, noise=0.05, seed=1)
@@ -53,6 +56,30 @@ def main():
     b, f = fused.cost()
     print(f"degree {a.degree} {a.prec} n={a.n} dof={box.l_size} tile={fused.tile()} {ms:.4f} ms/apply "
           f"{box.l_size / ms / 1e6:.3f} GDoF/s {b / ms / 1e6:.1f} GB/s(alg) {f / ms / 1e9:.3f} TFLOP/s alg_bytes={b:.0f}")
+
+
+def cg_case(a):
+    """FP64 CG and FP32 CG with FP64 refinement on the n^3 Poisson box with Dirichlet faces (smooth x*, b = A x*),
+    rtol 1e-10, graphs of 25 iterations: the solver kernels for a launch list."""
+    from libceed_gb300.solver import cg_solve
+
+    ceed = lc.Ceed("/gpu/cuda/b200", deterministic=a.det)
+    box = mesh.Box(a.n, a.degree, noise=0.05, seed=3)
+    o64 = build_poisson(ceed, box)
+    o32 = build_poisson(ceed, box, dtype=torch.float32)
+    m = mesh.box_mask(a.n, a.degree)
+    mask, xv, b = ceed.Vector(box.l_size), ceed.Vector(box.l_size), ceed.Vector(box.l_size)
+    mask.set_array(m)
+    xv.set_array(mesh.smooth_field(a.n, a.degree, seed=7) * m)
+    o64["op"].apply(xv, b)
+    b.set_array(m * b.get_array_read())
+    for mixed in (False, True):
+        x = ceed.Vector(box.l_size)
+        st = cg_solve(ceed, o64["op"], o64["qdata"], mask, b, x, mixed=mixed, op32=o32["op"], qdata32=o32["qdata"], rtol=1e-10,
+                      use_graph=True, check_every=25)
+        print(f"{'FP32+refinement' if mixed else 'FP64'} CG degree {a.degree} n={a.n} dof={box.l_size}: {st['iterations']} iterations, "
+              f"{st['outer']} outer, {st['seconds'] * 1e3:.2f} ms, {st['seconds'] * 1e3 / max(st['iterations'], 1):.4f} ms/iteration, "
+              f"rel. residual {st['rel_residual']:.2e}")
 
 
 if __name__ == "__main__":
