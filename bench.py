@@ -304,6 +304,8 @@ def gpu_main(a, rank, world, local_rank):
                      "compute": {"pipe": "fp64", "achieved": round(flops_alg / (kernel_ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s",
                                  "peak": round(fp64_peak, 4), "frac": round(flops_alg / (kernel_ms * 1e-3) / 1e12 / fp64_peak, 4),
                                  "algorithmic_flops": flops_alg,
+                                 "reference_model_flops": op.get_flops_estimate(),
+                                 "reference_model_tflops": round(op.get_flops_estimate() / (kernel_ms * 1e-3) / 1e12, 4),
                                  "peak_kind": "measured in this run (b200_fma_peak: independent FP64 FMA chains on every SM)"}},
         "cpu_baseline": {"value": round(cpu_rate, 5), "unit": "GDoF/s", "cores": cores, "kind": "port", "sample": sample},
         "clocks": clocks,

@@ -173,6 +173,12 @@ int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);
 int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add);
 /* Algorithmic bytes and FLOPs of one apply (for roofline reporting). */
 int b200_op_cost(b200_op op, double *bytes, double *flops);
+/* The reference's FLOP model of one apply of a fused operator, CeedOperatorGetFlopsEstimate
+ * (interface/ceed-operator.c:1834-1960, with CeedBasisGetFlopsEstimate at interface/ceed-basis.c:954 and
+ * CeedElemRestrictionGetFlopsEstimate at interface/ceed-elemrestriction.c:576, and the gallery QFunctions' estimates:
+ * Poisson 15, mass 1, times the components for the vector ones; the kappa-weighted Poisson, not in the gallery, 21).
+ * Pure host arithmetic (no GPU). */
+int b200_flops_estimate(int qf, int P_1d, int Q_1d, int num_comp, int64_t num_elem, int64_t *flops);
 /* Launch shape in use: elements per block and threads per block. */
 int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_per_block, int *staging);
 int b200_op_set_tile(b200_op op, int elems_per_block, int staging);

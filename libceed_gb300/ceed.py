@@ -566,6 +566,16 @@ class Operator:
         """CeedOperatorApplyAdd: v += A u."""
         self._apply(u, v, True)
 
+    def get_flops_estimate(self):
+        """CeedOperatorGetFlopsEstimate: the reference's FLOP model of one apply (b200_flops_estimate)."""
+        f = self._active_input()
+        kind = self.qf.kind
+        if not isinstance(kind, int):
+            raise B200Error("CeedOperatorGetFlopsEstimate", -2, "FLOP model available for the gallery apply QFunctions")
+        out = ctypes.c_int64()
+        call("b200_flops_estimate", kind, f.basis.P1d, f.basis.Q1d, f.rstr.ncomp, f.rstr.nelem, ctypes.byref(out))
+        return out.value
+
     def kappa_grad(self, u, w, g):
         """g[elem][qpt] = grad(w) . D grad(u): the kappa-adjoint of the kappa-weighted diffusion."""
         op = self._fused_op(u.prec)

@@ -355,6 +355,42 @@ extern "C" int b200_op_cost(b200_op op, double *bytes, double *flops) {
   return B200_SUCCESS;
 }
 
+// Tensor contraction FLOPs of one element and component block, as CeedBasisGetFlopsEstimate counts them
+// (interface/ceed-basis.c:971-977): sum over directions of 2 * pre * P * post * Q.
+static int64_t tensor_flops(int dim, int num_comp, int P, int Q) {
+  int64_t f = 0, pre = num_comp, post = 1;
+  for (int d = 0; d < dim - 1; d++) pre *= P;
+  for (int d = 0; d < dim; d++) {
+    f += 2 * pre * P * post * Q;
+    pre /= P;
+    post *= Q;
+  }
+  return f;
+}
+
+extern "C" int b200_flops_estimate(int qf, int P_1d, int Q_1d, int num_comp, int64_t num_elem, int64_t *flops) {
+  B200_CHECK(flops && P_1d >= 1 && Q_1d >= 1 && num_comp >= 1 && num_elem >= 0, B200_ERROR_DIMENSION, "b200_flops_estimate: bad arguments");
+  int64_t qf_flops = 0;
+  bool    grad     = true;
+  switch (qf) {
+    case B200_QF_MASS: qf_flops = 1, grad = false; break;
+    case B200_QF_POISSON: qf_flops = 15; break;
+    case B200_QF_VECMASS: qf_flops = num_comp, grad = false; break;
+    case B200_QF_VECPOISSON: qf_flops = 15 * num_comp; break;
+    case B200_QF_POISSON_KAPPA: qf_flops = 21; break;
+    default: B200_CHECK(false, B200_ERROR_UNSUPPORTED, "unknown QFunction %d", qf);
+  }
+  const int     dim  = 3;
+  const int64_t Q3   = (int64_t)Q_1d * Q_1d * Q_1d, P3 = (int64_t)P_1d * P_1d * P_1d;
+  const int64_t mult = grad ? 2 : 1;  // CEED_EVAL_GRAD counts twice the interpolation's tensor FLOPs
+  // The transposed basis counts with both 1D sizes set to Q_1d, as the reference's estimate does (its swap assigns
+  // P_1d = Q_1d and then Q_1d = P_1d).
+  const int64_t per_elem = mult * tensor_flops(dim, num_comp, P_1d, Q_1d) + Q3 * qf_flops + mult * tensor_flops(dim, num_comp, Q_1d, Q_1d) +
+                           P3 * num_comp;  // transposed restriction: one add per E-vector entry
+  *flops = num_elem ? num_elem * per_elem : 0;
+  return B200_SUCCESS;
+}
+
 extern "C" int b200_op_time(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int reps, double *ms_per_apply) {
   b200_ctx    ctx = op->ctx;
   cudaEvent_t e0, e1;

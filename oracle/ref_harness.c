@@ -239,6 +239,15 @@ static void case_operator(Ceed ceed, const op_case *c) {
   if (c->kappa) CeedOperatorSetField(op_apply, "kappa", rk, CEED_BASIS_NONE, KAP);
   CeedOperatorSetField(op_apply, c->poisson ? "dv" : "v", ru, bu, CEED_VECTOR_ACTIVE);
   CeedOperatorApply(op_apply, U, V, CEED_REQUEST_IMMEDIATE);
+  if (!c->kappa) {  // the reference's FLOP model (gallery QFunctions carry their estimates)
+    CeedSize flops = 0;
+    double   f;
+
+    CeedOperatorGetFlopsEstimate(op_apply, &flops);
+    f = (double)flops;
+    snprintf(name, sizeof name, "%s_flops", c->tag);
+    dump(name, "f64", &f, 1);
+  }
 
   snprintf(name, sizeof name, "%s_coords", c->tag);
   dump(name, "f64", coords, (size_t)(3 * nv));

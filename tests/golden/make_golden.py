@@ -49,7 +49,7 @@ def main():
     cases = sorted({k.rsplit("_", 1)[0] for k in arrays if k.endswith("_qdata")})
     for case in cases:
         out = {}
-        for key in ("qdata", "v", "kgrad", "kappa"):
+        for key in ("qdata", "v", "kgrad", "kappa", "flops"):
             if case + "_" + key in arrays:
                 out[key] = arrays[case + "_" + key]
         if case in FULL_ARRAYS:

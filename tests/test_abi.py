@@ -61,3 +61,29 @@ def test_ceed_refuses_without_gpu():
         ceed.Ceed("/gpu/cuda/b200")
     with pytest.raises(ceed.B200Error):
         ceed.Ceed("/cpu/self/ref/serial")
+
+
+def test_flops_estimate_matches_reference_model():
+    """b200_flops_estimate restates CeedOperatorGetFlopsEstimate; the golden fixtures hold the reference's values."""
+    import ctypes
+
+    import numpy as np
+
+    from libceed_gb300._ffi import call
+    from tests.conftest import GOLDEN
+    from tests.gpu_cases import CASES, parse
+
+    from libceed_gb300 import ceed as lcc
+
+    qf_of = {"mass": lcc.QF_MASS, "poisson": lcc.QF_POISSON, "vmass": lcc.QF_VECMASS, "vpoisson": lcc.QF_VECPOISSON}
+    checked = 0
+    for case in CASES:
+        g = np.load(f"{GOLDEN}/{case}.npz")
+        if "flops" not in g.files:
+            continue
+        kind, box = parse(case)
+        out = ctypes.c_int64()
+        call("b200_flops_estimate", qf_of[kind], box.P, box.Q, box.ncomp, box.num_elem, ctypes.byref(out))
+        assert out.value == int(g["flops"][0]), case
+        checked += 1
+    assert checked >= 10
