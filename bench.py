@@ -405,13 +405,15 @@ def run_vector_autotune(ceed, lc, mesh, build_poisson, torch):
     for p, n in ((2, 99), (4, 50), (6, 33)):
         box = mesh.Box(n, p, ncomp=3, noise=0.05, seed=5000 + p)
         for qf in ("Vector3Poisson3DApply", "Vector3MassApply"):
-            for dt in (torch.float32, torch.float64):
+            for tag, dt in (("f32", torch.float32), ("f64", torch.float64), ("f64x", torch.float64)):
                 objs = build_poisson(ceed, box, dtype=dt, qf_name=qf)
+                if tag == "f64x":
+                    objs["op"].arithmetic = "float-float"
                 u = ceed.Vector(box.l_size, dt)
                 u.set_array(box.u())
                 v = ceed.Vector(box.l_size, dt)
                 r = tune.autotune(objs["op"], u, v, reps=3, use_cache=False)
-                rows.append({"qfunction": qf, "degree": p, "P": box.P, "Q": box.Q, "ncomp": 3, "dtype": "f32" if dt == torch.float32 else "f64",
+                rows.append({"qfunction": qf, "degree": p, "P": box.P, "Q": box.Q, "ncomp": 3, "dtype": tag,
                              "nodes": box.num_nodes, "dof": box.l_size, "best": {"elems_per_block": r["epb"], "staging": r["staging"]},
                              "ms": r["ms"], "gdofs": round(box.l_size / r["ms"] / 1e6, 3), "candidates": len(r["sweep"])})
                 del objs, u, v

@@ -151,7 +151,7 @@ int b200_qdata_build(b200_ctx ctx, int poisson, int64_t num_elem, int Q_1d, cons
  *      kernel -> transposes -> scatter in one kernel per element batch. -------------------------------------------- */
 typedef struct {
   int            qf;          /* B200_QF_* */
-  int            prec;        /* B200_F64, B200_F32 or B200_F64X (mass and Poisson, centro-symmetric bases) */
+  int            prec;        /* B200_F64, B200_F32 or B200_F64X (centro-symmetric bases) */
   int            P_1d, Q_1d;  /* Q_1d = P_1d + 1 for the compiled kernels, P_1d in 2..9 */
   int            num_comp;    /* 1, or 3 for the vector QFunctions */
   int            scatter;     /* B200_SCATTER_ATOMIC or B200_SCATTER_DETERMINISTIC */

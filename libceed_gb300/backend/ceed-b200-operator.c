@@ -260,8 +260,8 @@ static int OperatorAnalyse_B200(CeedOperator op) {
       Ceed_B200 *data;
 
       CeedCallBackend(CeedGetData(ceed, &data));
-      // Float-float arithmetic where its kernels exist (scalar mass and Poisson, centro-symmetric bases); FP64 else.
-      if (data->float_float && (d.qf == B200_QF_MASS || d.qf == B200_QF_POISSON)) {
+      // Float-float arithmetic where its kernels exist (centro-symmetric bases); FP64 else.
+      if (data->float_float) {
         d.prec = B200_F64X;
         if (b200_op_create(ctx, &d, &impl->op)) d.prec = B200_F64;
       }

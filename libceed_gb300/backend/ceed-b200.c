@@ -49,8 +49,8 @@ static int CeedInit_B200(const char *resource, Ceed ceed) {
   CeedCallBackend(CeedFree(&resource_root));
   const char *dev = strstr(resource, ":device_id=");
   if (dev) device_id = atoi(dev + strlen(":device_id="));
-  // ":arithmetic=float-float": fused mass and Poisson applies on centro-symmetric bases run the float-float (B200_F64X)
-  // kernels on the same double vectors (within ~1e-13 relative of FP64); every other operator keeps FP64.
+  // ":arithmetic=float-float": fused applies on centro-symmetric bases run the float-float (B200_F64X) kernels on the
+  // same double vectors (within ~1e-13 relative of FP64); every other operator keeps FP64.
   const char *arith = strstr(resource, ":arithmetic=");
   CeedCheck(!arith || !strncmp(arith + strlen(":arithmetic="), "float-float", 11) || !strncmp(arith + strlen(":arithmetic="), "fp64", 4), ceed,
             CEED_ERROR_BACKEND, "B200 backend: arithmetic must be fp64 or float-float (resource %s)", resource);

@@ -425,18 +425,21 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   // ---- qdata staging ------------------------------------------------------------------------------------------------
   // Register staging keeps the loaded storage values (S) and converts at first use, so that the loads stay in flight
   // through the interpolation stages also when T is not the storage type.
-  constexpr int RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1;
-  S             rq[RQ][RZ];
+  // When T is the storage type kappa multiplies the qdata at load; otherwise it is kept apart and multiplied in T.
+  constexpr int  RQ = STAGE == kStageReg ? NQD : 1, RZ = STAGE == kStageReg ? Q : 1;
+  constexpr bool KSEP = TR::kappa && !__is_same(S, T);
+  S              rq[RQ][RZ];
+  S              rk[KSEP ? RZ : 1];
   if constexpr (STAGE == kStageReg) {
-    static_assert(!TR::kappa || __is_same(S, T), "kappa-weighted kernels compute in the storage type");
 #pragma unroll
     for (int z = 0; z < Q; z++) {
       S kap = S(1);
       if constexpr (TR::kappa) kap = active ? args.kappa[e * Q3 + B200_QLIN(a, b, z)] : S(0);
+      if constexpr (KSEP) rk[z] = kap;
 #pragma unroll
       for (int k = 0; k < NQD; k++) {
         rq[k][z] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + B200_QLIN(a, b, z)] : S(0);
-        if constexpr (TR::kappa) rq[k][z] *= kap;
+        if constexpr (TR::kappa && !KSEP) rq[k][z] *= kap;
       }
     }
   } else if constexpr (STAGE == kStageSmem) {
@@ -482,12 +485,14 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     }
   };
   auto qd = [&](int k, int z) -> T {
-    if constexpr (STAGE == kStageReg) return T(rq[k][z]);
-    else if constexpr (STAGE == kStageTma) {
+    if constexpr (STAGE == kStageReg) {
+      if constexpr (KSEP) return T(rq[k][z]) * T(rk[z]);
+      else return T(rq[k][z]);
+    } else if constexpr (STAGE == kStageTma) {
       const S  *sl  = reinterpret_cast<const S *>(smem_raw + 16);
       const int q   = slot * Q3 + B200_QLIN(a, b, z);
       const int st  = (int)(slab / sizeof(S));
-      if constexpr (TR::kappa) return T(sl[k * st + qoff[k] + q] * sl[NQD * st + qoff[NQD] + q]);
+      if constexpr (TR::kappa) return T(sl[k * st + qoff[k] + q]) * T(sl[NQD * st + qoff[NQD] + q]);
       else return T(sl[k * st + qoff[k] + q]);
     } else {
       const int q = B200_QLIN(a, b, z);

@@ -27,6 +27,9 @@ bool op_table_f32_vecpoisson(int, int, OpInstance *);
 bool op_table_f32_kappa(int, int, OpInstance *);
 bool op_table_f64x_mass(int, int, OpInstance *);
 bool op_table_f64x_poisson(int, int, OpInstance *);
+bool op_table_f64x_vecmass(int, int, OpInstance *);
+bool op_table_f64x_vecpoisson(int, int, OpInstance *);
+bool op_table_f64x_kappa(int, int, OpInstance *);
 bool kgrad_table_f64(int, OpLauncher *);
 bool kgrad_table_f32(int, OpLauncher *);
 
@@ -52,6 +55,9 @@ bool op_lookup(int prec, int qf, int P, int variant, OpInstance *out) {
     switch (qf) {
       case B200_QF_MASS: return op_table_f64x_mass(P, variant, out);
       case B200_QF_POISSON: return op_table_f64x_poisson(P, variant, out);
+      case B200_QF_VECMASS: return op_table_f64x_vecmass(P, variant, out);
+      case B200_QF_VECPOISSON: return op_table_f64x_vecpoisson(P, variant, out);
+      case B200_QF_POISSON_KAPPA: return op_table_f64x_kappa(P, variant, out);
     }
   }
   return false;
@@ -227,8 +233,6 @@ static int op_select(b200_op op, int epb, int stage) {
 extern "C" int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *out) {
   const b200_op_desc &d = *desc;
   B200_CHECK(d.prec == B200_F64 || d.prec == B200_F32 || d.prec == B200_F64X, B200_ERROR_UNSUPPORTED, "unknown precision %d", d.prec);
-  B200_CHECK(d.prec != B200_F64X || d.qf == B200_QF_MASS || d.qf == B200_QF_POISSON, B200_ERROR_UNSUPPORTED,
-             "float-float kernels cover the scalar mass and Poisson QFunctions");
   B200_CHECK(d.Q_1d == d.P_1d + 1, B200_ERROR_UNSUPPORTED, "fused kernels are compiled for Q_1d = P_1d + 1 (got P=%d, Q=%d)", d.P_1d, d.Q_1d);
   B200_CHECK(d.P_1d >= kOpPMin && d.P_1d <= kOpPMax, B200_ERROR_UNSUPPORTED, "fused kernels cover P_1d in %d..%d (got %d)", kOpPMin, kOpPMax, d.P_1d);
   const int nc_expected = (d.qf == B200_QF_VECMASS || d.qf == B200_QF_VECPOISSON) ? 3 : 1;
