@@ -642,7 +642,7 @@ struct Op3DShape {
 // a length-P or length-Q dot product over a shared tile.  Same stages and result as k_op_apply (general, not even-odd
 // contractions); every thread reads its own point's qdata once.
 template <typename T, int P, int Q, int QF>
-__global__ void k_op_apply_3d(const OpArgs<T> args, const OpMats<T, P, Q> M) {
+__global__ void k_op_apply_3d(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
   using TR         = QFTraits<QF>;
   using SH         = Op3DShape<T, P, Q>;
   constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P2 = P * P, P3 = P * P * P, NC = TR::nc, NQD = TR::nqd;
@@ -659,61 +659,75 @@ __global__ void k_op_apply_3d(const OpArgs<T> args, const OpMats<T, P, Q> M) {
   T         D[NQD];
   {
     T kap = T(1);
-    if constexpr (TR::kappa) kap = active ? args.kappa[e * Q3 + t] : T(0);
+    if constexpr (TR::kappa) kap = active ? T(args.kappa[e * Q3 + t]) : T(0);
 #pragma unroll
-    for (int k = 0; k < NQD; k++) D[k] = active ? args.qdata[((int64_t)k * ne + e) * Q3 + t] * kap : T(0);
+    for (int k = 0; k < NQD; k++) D[k] = active ? T(args.qdata[((int64_t)k * ne + e) * Q3 + t]) * kap : T(0);
   }
   const int32_t my_off = (active && t < P3) ? args.offsets[e * P3 + t] : 0;
 
 #pragma unroll 1
   for (int c = 0; c < NC; c++) {
     __syncthreads();  // matrices in place (c = 0), tiles free again (c > 0)
-    if (t < P3) s0[B200_IDX(t % P, (t / P) % P, t / P2)] = active ? args.u[(int64_t)my_off + c * args.comp_stride] : T(0);
+    if (t < P3) s0[B200_IDX(t % P, (t / P) % P, t / P2)] = active ? T(args.u[(int64_t)my_off + c * args.comp_stride]) : T(0);
     __syncthreads();
     if (t < Q * P2) {  // X interpolation: (i < Q, j < P, k < P)
       const int i = t % Q, j = (t / Q) % P, k = t / (Q * P);
-      T         s = T(0);
+      Dot<T>    s;
+      s.first(sB[i * P], s0[B200_IDX(0, j, k)]);
 #pragma unroll
-      for (int m = 0; m < P; m++) s = mad(sB[i * P + m], s0[B200_IDX(m, j, k)], s);
-      s1[B200_IDX(i, j, k)] = s;
+      for (int m = 1; m < P; m++) s.add(sB[i * P + m], s0[B200_IDX(m, j, k)]);
+      s1[B200_IDX(i, j, k)] = s.value();
     }
     __syncthreads();
     if (t < Q2 * P) {  // Y interpolation: (i < Q, j < Q, k < P)
       const int i = t % Q, j = (t / Q) % Q, k = t / Q2;
-      T         s = T(0);
+      Dot<T>    s;
+      s.first(sB[j * P], s1[B200_IDX(i, 0, k)]);
 #pragma unroll
-      for (int m = 0; m < P; m++) s = mad(sB[j * P + m], s1[B200_IDX(i, m, k)], s);
-      s0[B200_IDX(i, j, k)] = s;
+      for (int m = 1; m < P; m++) s.add(sB[j * P + m], s1[B200_IDX(i, m, k)]);
+      s0[B200_IDX(i, j, k)] = s.value();
     }
     __syncthreads();
-    T U = T(0);  // Z interpolation: every point
+    T U;  // Z interpolation: every point
+    {
+      Dot<T> s;
+      s.first(sB[z * P], s0[B200_IDX(x, y, 0)]);
 #pragma unroll
-    for (int m = 0; m < P; m++) U = mad(sB[z * P + m], s0[B200_IDX(x, y, m)], U);
+      for (int m = 1; m < P; m++) s.add(sB[z * P + m], s0[B200_IDX(x, y, m)]);
+      U = s.value();
+    }
     T w;
     if constexpr (TR::grad) {
       s1[B200_IDX(x, y, z)] = U;
       __syncthreads();
-      T g0 = T(0), g1 = T(0), g2 = T(0);
+      Dot<T> d0, d1, d2;
+      d0.first(sG[x * Q], s1[B200_IDX(0, y, z)]);
+      d1.first(sG[y * Q], s1[B200_IDX(x, 0, z)]);
+      d2.first(sG[z * Q], s1[B200_IDX(x, y, 0)]);
 #pragma unroll
-      for (int m = 0; m < Q; m++) {
-        g0 = mad(sG[x * Q + m], s1[B200_IDX(m, y, z)], g0);
-        g1 = mad(sG[y * Q + m], s1[B200_IDX(x, m, z)], g1);
-        g2 = mad(sG[z * Q + m], s1[B200_IDX(x, y, m)], g2);
+      for (int m = 1; m < Q; m++) {
+        d0.add(sG[x * Q + m], s1[B200_IDX(m, y, z)]);
+        d1.add(sG[y * Q + m], s1[B200_IDX(x, m, z)]);
+        d2.add(sG[z * Q + m], s1[B200_IDX(x, y, m)]);
       }
       T vg[3];
-      poisson_point(D, g0, g1, g2, vg);
+      poisson_point(D, d0.value(), d1.value(), d2.value(), vg);
       __syncthreads();
       s0[B200_IDX(x, y, z)] = vg[0];
       s1[B200_IDX(x, y, z)] = vg[1];
       s2[B200_IDX(x, y, z)] = vg[2];
       __syncthreads();
-      w = T(0);
+      Dot<T> dw;
+      dw.first(sG[x], s0[B200_IDX(0, y, z)]);
+      dw.add(sG[y], s1[B200_IDX(x, 0, z)]);
+      dw.add(sG[z], s2[B200_IDX(x, y, 0)]);
 #pragma unroll
-      for (int m = 0; m < Q; m++) {
-        w = mad(sG[m * Q + x], s0[B200_IDX(m, y, z)], w);
-        w = mad(sG[m * Q + y], s1[B200_IDX(x, m, z)], w);
-        w = mad(sG[m * Q + z], s2[B200_IDX(x, y, m)], w);
+      for (int m = 1; m < Q; m++) {
+        dw.add(sG[m * Q + x], s0[B200_IDX(m, y, z)]);
+        dw.add(sG[m * Q + y], s1[B200_IDX(x, m, z)]);
+        dw.add(sG[m * Q + z], s2[B200_IDX(x, y, m)]);
       }
+      w = dw.value();
     } else {
       w = U * D[0];
     }
@@ -722,27 +736,31 @@ __global__ void k_op_apply_3d(const OpArgs<T> args, const OpMats<T, P, Q> M) {
     __syncthreads();
     if (t < Q2 * P) {  // Z interpolation transposed: (i < Q, j < Q, k < P)
       const int i = t % Q, j = (t / Q) % Q, k = t / Q2;
-      T         s = T(0);
+      Dot<T>    s;
+      s.first(sB[k], s0[B200_IDX(i, j, 0)]);
 #pragma unroll
-      for (int m = 0; m < Q; m++) s = mad(sB[m * P + k], s0[B200_IDX(i, j, m)], s);
-      s1[B200_IDX(i, j, k)] = s;
+      for (int m = 1; m < Q; m++) s.add(sB[m * P + k], s0[B200_IDX(i, j, m)]);
+      s1[B200_IDX(i, j, k)] = s.value();
     }
     __syncthreads();
     if (t < Q * P2) {  // Y interpolation transposed: (i < Q, j < P, k < P)
       const int i = t % Q, j = (t / Q) % P, k = t / (Q * P);
-      T         s = T(0);
+      Dot<T>    s;
+      s.first(sB[j], s1[B200_IDX(i, 0, k)]);
 #pragma unroll
-      for (int m = 0; m < Q; m++) s = mad(sB[m * P + j], s1[B200_IDX(i, m, k)], s);
-      s0[B200_IDX(i, j, k)] = s;
+      for (int m = 1; m < Q; m++) s.add(sB[m * P + j], s1[B200_IDX(i, m, k)]);
+      s0[B200_IDX(i, j, k)] = s.value();
     }
     __syncthreads();
     if (t < P3 && active) {  // X interpolation transposed and scatter: node (i, j, k) = t
       const int i = t % P, j = (t / P) % P, k = t / P2;
-      T         s = T(0);
+      Dot<T>    s;
+      s.first(sB[i], s0[B200_IDX(0, j, k)]);
 #pragma unroll
-      for (int m = 0; m < Q; m++) s = mad(sB[m * P + i], s0[B200_IDX(m, j, k)], s);
-      if (args.det) args.e_out[((int64_t)c * ne + e) * P3 + t] = s;
-      else atomicAdd(&args.v[(int64_t)my_off + c * args.comp_stride], s);
+      for (int m = 1; m < Q; m++) s.add(sB[m * P + i], s0[B200_IDX(m, j, k)]);
+      using S = typename Store<T>::type;
+      if (args.det) args.e_out[((int64_t)c * ne + e) * P3 + t] = (S)s.value();
+      else atomicAdd(&args.v[(int64_t)my_off + c * args.comp_stride], (S)s.value());
     }
   }
 }

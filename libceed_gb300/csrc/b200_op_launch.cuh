@@ -207,6 +207,7 @@ bool op_variant(int variant, OpInstance *out) {
     if (variant == kVarRegEO) *out = op_instance<T, P, QF, kStageReg, true>();
     else if (variant == kVarSmemEO) *out = op_instance<T, P, QF, kStageSmem, true>();
     else if (variant == kVarTmaEO) *out = op_instance<T, P, QF, kStageTma, true>();
+    else if (variant == kVar3D) *out = op_instance_3d<T, P, QF>();
     else return false;
     return true;
   } else {
