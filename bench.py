@@ -220,6 +220,8 @@ def gpu_main(a, rank, world, local_rank):
     torch.cuda.synchronize()
     kernel_ms = k0.elapsed_time(k1) / a.steps
     fp64_peak = ceed.fma_peak(lc.F64)  # the fused FP64 kernel is bound by this pipe, not by HBM
+    # FP64 tensor cores (DMMA): rate alone and interleaved with DFMA; no gain over fp64_peak means one shared FP64 unit.
+    dmma_tflops, dmma_mixed_tflops = ceed.fp64_tensor_peak()
 
     # End to end through the public API: every step copies its input from pinned host memory to the device, applies the
     # operator and copies the result back to pinned host memory.  Double-buffered on three streams, so that the
@@ -306,7 +308,9 @@ def gpu_main(a, rank, world, local_rank):
                                  "algorithmic_flops": flops_alg,
                                  "reference_model_flops": op.get_flops_estimate(),
                                  "reference_model_tflops": round(op.get_flops_estimate() / (kernel_ms * 1e-3) / 1e12, 4),
-                                 "peak_kind": "measured in this run (b200_fma_peak: independent FP64 FMA chains on every SM)"}},
+                                 "peak_kind": "measured in this run (b200_fma_peak: independent FP64 FMA chains on every SM)",
+                                 "fp64_tensor": {"dmma_tflops": round(dmma_tflops, 4), "dmma_plus_dfma_tflops": round(dmma_mixed_tflops, 4),
+                                                 "note": "mma.sync m8n8k4 f64 alone, and interleaved with DFMA chains in every warp (b200_fp64_tensor_peak)"}}},
         "cpu_baseline": {"value": round(cpu_rate, 5), "unit": "GDoF/s", "cores": cores, "kind": "port", "sample": sample},
         "clocks": clocks,
     }

@@ -273,6 +273,12 @@ int b200_cg_solve(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64,
  *      compute-bound kernels report a fraction of a measured peak.  Blocks the host; *tflops = 2 * FMAs / s / 1e12. */
 int b200_fma_peak(b200_ctx ctx, int prec, double *tflops);
 
+/* ---- FP64 tensor-core probe.  No counterpart in the reference: *dmma_tflops is the FP64 rate of the tensor-core
+ *      instruction mma.sync m8n8k4 (DMMA) alone; *mixed_tflops the total FP64 rate when every warp interleaves DMMA
+ *      chains with DFMA chains.  A mixed rate no higher than the larger single rate means the two share one FP64 unit,
+ *      so moving contractions of the FP64 kernels onto the tensor path cannot raise their bound.  Blocks the host. */
+int b200_fp64_tensor_peak(b200_ctx ctx, double *dmma_tflops, double *mixed_tflops);
+
 #ifdef __cplusplus
 }
 #endif

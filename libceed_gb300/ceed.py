@@ -107,6 +107,12 @@ class Ceed:
         call("b200_fma_peak", self._ctx, prec, ctypes.byref(t))
         return t.value
 
+    def fp64_tensor_peak(self):
+        """(DMMA-only, DMMA+DFMA interleaved) FP64 TFLOP/s: whether the FP64 tensor path adds to the FP64 FMA pipe."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        call("b200_fp64_tensor_peak", self._ctx, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
     def gauss_quadrature(self, q):
         return basis1d.gauss_quadrature(q)
 

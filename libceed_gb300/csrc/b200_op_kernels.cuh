@@ -149,15 +149,27 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
   return false;
 }
 
-// Shared-memory prefix of the bulk-copy staging: an mbarrier (16 bytes) and one slab per staged qdata component of
-// epb*Q^3 storage values plus 16 bytes of alignment slack on each side.
-template <typename S, int Q3>
-__host__ __device__ constexpr size_t tma_slab_bytes(int epb) {
-  return ((size_t)epb * Q3 * sizeof(S) + 32 + 15) / 16 * 16;
+// Element stride (storage values) of a bulk-copy qdata slab copied element by element: the smallest stride >= Q^3 that
+// is a multiple of 16 bytes and that continues the team's point index Q^2 modulo the bank width (32 four-byte banks;
+// 8-byte values go in half-warps over 16 bank pairs).  Then a warp whose lanes span two teams reads consecutive banks in
+// the pointwise stage instead of two overlapping runs.
+template <typename S, int Q>
+__host__ __device__ constexpr int tma_elem_stride() {
+  constexpr int W = 128 / (int)sizeof(S), A = 16 / (int)sizeof(S);
+  if ((Q * Q) % A != 0) return Q * Q * Q;  // no such stride (odd Q: elements are not 16-byte aligned either)
+  int sq = Q * Q * Q;
+  while (sq % A != 0 || (sq - Q * Q) % W != 0) sq++;
+  return sq;
 }
-template <typename S, int Q3, int NQK>
+// Shared-memory prefix of the bulk-copy staging: an mbarrier (16 bytes) and one slab per staged qdata component of
+// epb elements (element stride tma_elem_stride) plus 16 bytes of alignment slack on each side.
+template <typename S, int Q>
+__host__ __device__ constexpr size_t tma_slab_bytes(int epb) {
+  return ((size_t)epb * tma_elem_stride<S, Q>() * sizeof(S) + 32 + 15) / 16 * 16;
+}
+template <typename S, int Q, int NQK>
 __host__ __device__ constexpr size_t tma_prefix_bytes(int epb) {
-  return 16 + NQK * tma_slab_bytes<S, Q3>(epb);
+  return 16 + NQK * tma_slab_bytes<S, Q>(epb);
 }
 
 struct NoWait {
@@ -255,19 +267,21 @@ struct Contract {
 #define B200_IDX(x, y, z) ((x) + Q * (y) + tile_plane(Q) * (z))  // shared-memory tile position
 #define B200_QLIN(x, y, z) ((x) + Q * ((y) + Q * (z)))         // linear point index of global arrays
 
-// The element pipeline from the gathered tile to the thread's output line.  On entry s0[IDX(x,y,z)] holds the element
-// values (x, y, z < P) and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata
-// component k (kappa already applied) at point (a, b, z).  On exit, threads with a, b < P hold in out[p] the element
-// result at node (p, a, b).  Uses s0, s1, s2 (Q^3 each) and block-wide barriers.
-template <typename T, int P, int Q, int QF, bool EO, typename QD, typename QW = NoWait>
-__device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P, Q> &M, int a, int b, QD qd, T (&out)[P], QW qwait = QW{}) {
+// The element pipeline from the gathered element values to the thread's output line.  On entry either (XREG) threads
+// with a, b < P hold in xin[p] the element value at node (p, a, b), or s0[IDX(x,y,z)] holds the element values
+// (x, y, z < P) and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata component k
+// (kappa already applied) at point (a, b, z).  On exit, threads with a, b < P hold in out[p] the element result at node
+// (p, a, b).  Uses s0, s1, s2 (Q^3 each) and block-wide barriers.
+template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename QD, typename QW = NoWait>
+__device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P, Q> &M, int a, int b, const T (&xin)[P], QD qd, T (&out)[P],
+                                          QW qwait = QW{}) {
   using C             = Contract<T, P, Q, EO>;
   constexpr bool GRAD = QFTraits<QF>::grad;
   // ---- X interpolation: lines (y, z) < P --------------------------------------------------------------------------
   if (a < P && b < P) {
     T in[P], o[Q];
 #pragma unroll
-    for (int k = 0; k < P; k++) in[k] = s0[B200_IDX(k, a, b)];
+    for (int k = 0; k < P; k++) in[k] = XREG ? xin[k] : s0[B200_IDX(k, a, b)];
     C::interp(M, in, o);
 #pragma unroll
     for (int j = 0; j < Q; j++) s1[B200_IDX(j, a, b)] = o[j];
@@ -418,7 +432,7 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   using S              = typename Store<T>::type;
   constexpr int NQK    = TR::nqk;
   // Bulk-copy staging: [mbarrier][NQK slabs][team tiles]; the other stagings start with the team tiles.
-  const size_t       prefix = STAGE == kStageTma ? tma_prefix_bytes<S, Q3, NQK>(args.epb) : 0;
+  const size_t       prefix = STAGE == kStageTma ? tma_prefix_bytes<S, Q, NQK>(args.epb) : 0;
   unsigned long long *bar   = reinterpret_cast<unsigned long long *>(smem_raw);
   T *s0 = reinterpret_cast<T *>(smem_raw + prefix) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q), *sq = s2 + tile_buf(Q);
 
@@ -450,30 +464,48 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     if constexpr (TR::kappa)
       for (int q = tid; q < Q3; q += Q2) sq[NQD * Q3 + q] = active ? T(args.kappa[e * Q3 + q]) : T(0);
   }
-  // Bulk-copy staging: slab k holds component k (kappa last) of the block's elements e0 .. e0 + nb - 1.  A range that
-  // does not start or end on 16 bytes is widened to the enclosing 16-byte chunks (each chunk holds array data, so it
-  // lies on a mapped page); qoff[k] is the offset, in storage values, of element e0 within slab k.
-  const int64_t e0   = (int64_t)blockIdx.x * args.epb;
-  const int     nb   = (int)((ne - e0) < args.epb ? (ne - e0) : args.epb);
-  const size_t  slab = tma_slab_bytes<S, Q3>(args.epb);
-  int           qoff[STAGE == kStageTma ? NQK : 1];
+  // Bulk-copy staging: slab k holds component k (kappa last) of the block's elements e0 .. e0 + nb - 1.  When every
+  // element's range starts on 16 bytes (Q^3 values of 16-byte multiple size, aligned arrays) each element is copied on
+  // its own to a padded element stride (tma_elem_stride: consecutive banks for warps spanning two teams); the lanes of
+  // warp 0 share the nqk * nb copies.  Otherwise each component is one copy of the block's contiguous range, widened to
+  // the enclosing 16-byte chunks (each chunk holds array data, so it lies on a mapped page); qoff[k] is then the offset,
+  // in storage values, of element e0 within slab k.
+  const int64_t  e0    = (int64_t)blockIdx.x * args.epb;
+  const int      nb    = (int)((ne - e0) < args.epb ? (ne - e0) : args.epb);
+  const size_t   slab  = tma_slab_bytes<S, Q>(args.epb);
+  constexpr int  SQ    = tma_elem_stride<S, Q>();
+  const bool     split = (Q3 * sizeof(S)) % 16 == 0 && (((size_t)args.qdata | (size_t)args.kappa) & 15) == 0;
+  const int      estr  = split ? SQ : Q3;  // element stride within a slab
+  int            qoff[STAGE == kStageTma ? NQK : 1];
+  auto           comp_src = [&](int k, int64_t el) -> const S * {
+    return (TR::kappa && k == NQD) ? args.kappa + el * Q3 : args.qdata + ((int64_t)k * ne + el) * Q3;
+  };
   if constexpr (STAGE == kStageTma) {
 #pragma unroll
-    for (int k = 0; k < NQK; k++) {
-      const S *src = (TR::kappa && k == NQD) ? args.kappa + e0 * Q3 : args.qdata + ((int64_t)k * ne + e0) * Q3;
-      qoff[k]      = (int)(((size_t)src & 15) / sizeof(S));
-    }
-    if (threadIdx.x == 0) {
+    for (int k = 0; k < NQK; k++) qoff[k] = split ? 0 : (int)(((size_t)comp_src(k, e0) & 15) / sizeof(S));
+    if (split) {
+      if (threadIdx.x < 32) {
+        if (threadIdx.x == 0) {
+          mbar_init(bar, 1);
+          mbar_arrive_expect_tx(bar, (unsigned)(NQK * nb * Q3 * sizeof(S)));
+        }
+        __syncwarp();
+        for (int i = threadIdx.x; i < NQK * nb; i += 32) {
+          const int k = i / nb, el = i % nb;
+          bulk_copy_g2s(smem_raw + 16 + k * slab + (size_t)el * SQ * sizeof(S), comp_src(k, e0 + el), (unsigned)(Q3 * sizeof(S)), bar);
+        }
+      }
+    } else if (threadIdx.x == 0) {
       mbar_init(bar, 1);
       unsigned total = 0;
       for (int k = 0; k < NQK; k++) {
-        const S     *src = (TR::kappa && k == NQD) ? args.kappa + e0 * Q3 : args.qdata + ((int64_t)k * ne + e0) * Q3;
+        const S     *src = comp_src(k, e0);
         const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
         total += (unsigned)(hi - lo);
       }
       mbar_arrive_expect_tx(bar, total);
       for (int k = 0; k < NQK; k++) {
-        const S     *src = (TR::kappa && k == NQD) ? args.kappa + e0 * Q3 : args.qdata + ((int64_t)k * ne + e0) * Q3;
+        const S     *src = comp_src(k, e0);
         const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
         bulk_copy_g2s(smem_raw + 16 + k * slab, (const void *)lo, (unsigned)(hi - lo), bar);
       }
@@ -490,7 +522,7 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
       else return T(rq[k][z]);
     } else if constexpr (STAGE == kStageTma) {
       const S  *sl  = reinterpret_cast<const S *>(smem_raw + 16);
-      const int q   = slot * Q3 + B200_QLIN(a, b, z);
+      const int q   = slot * estr + B200_QLIN(a, b, z);
       const int st  = (int)(slab / sizeof(S));
       if constexpr (TR::kappa) return T(sl[k * st + qoff[k] + q]) * T(sl[NQD * st + qoff[NQD] + q]);
       else return T(sl[k * st + qoff[k] + q]);
@@ -501,25 +533,63 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     }
   };
 
-  // Thread (a, b), a, b < P, gathers and later scatters the element's x-line of nodes (p, a, b): its P offsets stay
-  // in registers from the gather to the scatter.
-  const bool owner = a < P && b < P;
-  int32_t    off_line[P];
+  // Coalesced gather and scatter (FP32, bulk-copy staging): team thread tid handles the element's nodes i = tid + r Q^2
+  // in lexicographic order, so a warp's loads and atomics touch runs of consecutive nodes; the values pass through
+  // shared memory on the way to and from the x-line owners.  This pays where the L1 data pipe is the bound (the FP32
+  // kernels); the FP64 and float-float kernels, bound by their arithmetic, keep the other form: thread (a, b),
+  // a, b < P, gathers and later scatters the element's x-line of nodes (p, a, b), which feeds the X interpolation from
+  // registers.  Either way the thread's offsets stay in registers from the gather to the scatter.
+  constexpr bool CG = STAGE == kStageTma && __is_same(T, float);
+  constexpr int  PU = (P3 + Q2 - 1) / Q2;  // nodes per thread in the coalesced form
+  const bool     owner = a < P && b < P;
+  int32_t        off_line[CG ? PU : P];
+  if constexpr (CG) {
 #pragma unroll
-  for (int p = 0; p < P; p++) off_line[p] = (owner && active) ? args.offsets[e * P3 + P * (a + P * b) + p] : 0;
+    for (int r = 0; r < PU; r++) off_line[r] = (active && tid + r * Q2 < P3) ? args.offsets[e * P3 + tid + r * Q2] : 0;
+  } else {
+#pragma unroll
+    for (int p = 0; p < P; p++) off_line[p] = (owner && active) ? args.offsets[e * P3 + P * (a + P * b) + p] : 0;
+  }
 
+  // The barrier at the top of each later component protects the tiles still being read by the previous one.
 #pragma unroll 1
   for (int c = 0; c < NC; c++) {
     if (c > 0) __syncthreads();
-    if (owner) {
+    T xin[P], out[P];
+    if constexpr (CG) {
 #pragma unroll
-      for (int p = 0; p < P; p++) s0[B200_IDX(p, a, b)] = active ? T(args.u[(int64_t)off_line[p] + c * args.comp_stride]) : T(0);
+      for (int r = 0; r < PU; r++) {
+        const int i = tid + r * Q2;
+        if (i < P3) s0[B200_IDX(i % P, (i / P) % P, i / (P * P))] = active ? T(args.u[(int64_t)off_line[r] + c * args.comp_stride]) : T(0);
+      }
+      __syncthreads();
+      if (c == 0) op_stages<T, P, Q, QF, EO, false>(s0, s1, s2, M, a, b, xin, qd, out, qwait);
+      else op_stages<T, P, Q, QF, EO, false>(s0, s1, s2, M, a, b, xin, qd, out);
+      // s0 was last read by the Y interpolation (transposed), before the barrier that preceded the X stage.
+      if (owner) {
+#pragma unroll
+        for (int p = 0; p < P; p++) s0[B200_IDX(p, a, b)] = out[p];
+      }
+      __syncthreads();
+      if (active) {
+        using S = typename Store<T>::type;
+#pragma unroll
+        for (int r = 0; r < PU; r++) {
+          const int i = tid + r * Q2;
+          if (i < P3) {
+            const T val = s0[B200_IDX(i % P, (i / P) % P, i / (P * P))];
+            if (args.det) args.e_out[((int64_t)c * ne + e) * P3 + i] = (S)val;
+            else atomicAdd(&args.v[(int64_t)off_line[r] + c * args.comp_stride], (S)val);
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p < P; p++) xin[p] = (owner && active) ? T(args.u[(int64_t)off_line[p] + c * args.comp_stride]) : T(0);
+      if (c == 0) op_stages<T, P, Q, QF, EO, true>(s0, s1, s2, M, a, b, xin, qd, out, qwait);
+      else op_stages<T, P, Q, QF, EO, true>(s0, s1, s2, M, a, b, xin, qd, out);
+      if (owner && active) scatter_line<T, P>(args, e, c, off_line, a, b, out);
     }
-    __syncthreads();
-    T out[P];
-    if (c == 0) op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out, qwait);
-    else op_stages<T, P, Q, QF, EO>(s0, s1, s2, M, a, b, qd, out);
-    if (owner && active) scatter_line<T, P>(args, e, c, off_line, a, b, out);
   }
 }
 
@@ -621,8 +691,8 @@ __global__ void k_op_apply_pipe(const OpArgs<typename Store<T>::type> args, cons
       if constexpr (TR::kappa) return sq[k * Q3 + q] * sq[NQD * Q3 + q];
       else return sq[k * Q3 + q];
     };
-    T out[P];
-    op_stages<T, P, Q, QF, true>(s0, s1, s2, M, a, b, qd, out);
+    T out[P], none[P];
+    op_stages<T, P, Q, QF, true, false>(s0, s1, s2, M, a, b, none, qd, out);
     if (a < P && b < P && active) scatter_line<T, P>(args, e, 0, soff + P * (a + P * b), a, b, out);
     buf ^= 1;
   }

@@ -94,7 +94,7 @@ template <typename T, int P, int QF, int STAGE>
 size_t op_smem(int epb) {
   constexpr int Q = P + 1;
   size_t        prefix = 0;
-  if constexpr (STAGE == kStageTma) prefix = tma_prefix_bytes<typename Store<T>::type, Q * Q * Q, QFTraits<QF>::nqk>(epb);
+  if constexpr (STAGE == kStageTma) prefix = tma_prefix_bytes<typename Store<T>::type, Q, QFTraits<QF>::nqk>(epb);
   return prefix + sizeof(T) * (size_t)epb * OpShape<T, P, Q, QF, STAGE>::team_smem;
 }
 

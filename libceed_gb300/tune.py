@@ -100,7 +100,7 @@ def sweep_main(argv=None):
     """Tile sweep of the scalar Poisson and mass operators over degrees and kernel families; one JSON line per
     (degree, QFunction, family) with the best tile and the best rate of every staging.  Needs a GPU.
 
-        python -m libceed_gb300.tune --degrees 1,2,3,4,5,6,7,8
+        python -m libceed_gb300.tune --degrees 1,2,3,4,5,6,7,8 [--families f64,f32,f64x] [--qfunctions Poisson3DApply,MassApply]
     """
     import argparse
 
@@ -113,12 +113,17 @@ def sweep_main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--degrees", default="1,2,3,4,5,6,7,8")
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--families", default="f64,f32,f64x", help="comma-separated subset of f64, f32, f64x")
+    ap.add_argument("--qfunctions", default="Poisson3DApply,MassApply")
     a = ap.parse_args(argv)
+    families = a.families.split(",")
     ceed = Ceed("/gpu/cuda/b200")
     for p in [int(x) for x in a.degrees.split(",")]:
         box = mesh.Box(BOX_N[p], p, noise=0.05, seed=5)
-        for qf in ("Poisson3DApply", "MassApply"):
+        for qf in a.qfunctions.split(","):
             for tag, dt, arith in (("f64", torch.float64, "native"), ("f32", torch.float32, "native"), ("f64x", torch.float64, "float-float")):
+                if tag not in families:
+                    continue
                 objs = build_poisson(ceed, box, dtype=dt, qf_name=qf)
                 op = objs["op"]
                 op.arithmetic = arith

@@ -106,3 +106,11 @@ def test_gallery_qfunction_apply(ceed):
     ug = du.reshape(3, n)
     want = np.einsum("ijn,in->jn", M, ug).reshape(-1)
     assert relinf(out.get_array_read(), want) < 1e-14
+
+
+def test_pipe_probes_report_positive_rates(ceed):
+    # The compute-roofline denominators: FP64 and FP32 FMA rates, and the FP64 tensor-core (DMMA) rate alone and
+    # interleaved with DFMA in every warp.
+    assert ceed.fma_peak(lc.F64) > 0 and ceed.fma_peak(lc.F32) > 0
+    dmma, mixed = ceed.fp64_tensor_peak()
+    assert dmma > 0 and mixed > 0
