@@ -65,6 +65,94 @@ __host__ __device__ constexpr int tile_team_stride(int Q, int extra) {
   return 3 * tile_buf(Q) + extra + ((tile_team_mod(Q) - (3 * tile_buf(Q) + extra) % 32) % 32 + 32) % 32;
 }
 
+// Per-epoch tile layouts.  An epoch is the life of one tile buffer's contents, from the stage that writes it to the
+// last stage that reads it; its layout places point (x, y, z) of team `slot` at slot*sg + x*sx + y*sy + z*sz within the
+// buffer's region.  Lanes of one warp are consecutive team threads, and each stage's accesses run along one direction
+// (x-lines, y-lines, z-lines, or the element's nodes in lexicographic order for the coalesced gather and scatter), so a
+// layout can be conflict-free for the writer's direction and the reader's direction together where one fixed layout
+// cannot serve all three.  The FP32 bulk-copy kernels (coalesced gather and scatter) use layouts chosen per (Q, epoch)
+// by a search over axis orders, paddings and team strides that minimises a model of the shared-memory wavefronts (32
+// four-byte banks) of every stage at the default tile, with extents within 12% of Q^3: e.g. at Q = 6 the model counts
+// 16% fewer wavefronts than the single padded layout, at Q = 8 32% fewer (measured: 0-4% faster applies; the address
+// arithmetic costs registers, which is why the register-staged kernels, limited by occupancy, keep the single layout
+// above, as do the FP64 and float-float kernels).
+enum { kEpGather = 0, kEpXY, kEpYZ, kEpU, kEpDX, kEpDY, kEpT, kEpZT, kEpYT, kEpScatter, kNumEp };
+
+struct TileLay {
+  int sx, sy, sz, sg, ext;  // strides of x, y, z and of the team slot; extent of one team's tile
+};
+
+// Epoch order: gather (nodes -> X interpolation), X -> Y interpolation, Y -> Z interpolation, interpolated values ->
+// X and Y derivatives, X derivative -> QFunction -> transposed X derivative, the same for Y, transposed X -> Y -> Z
+// derivatives, transposed Z -> Y interpolation, transposed Y -> X interpolation, X-line results -> scatter.
+__host__ __device__ constexpr TileLay tile_lay_f32(int Q, int ep) {
+  constexpr TileLay t[8][kNumEp] = {
+      {{1, 3, 9, 27, 27}, {1, 10, 3, 38, 29}, {3, 1, 9, 27, 27}, {1, 3, 9, 27, 27}, {1, 3, 9, 27, 27},
+       {3, 1, 9, 27, 27}, {3, 1, 9, 27, 27}, {3, 1, 9, 27, 27}, {1, 10, 3, 38, 29}, {1, 3, 9, 27, 27}},  // Q = 3
+      {{1, 4, 17, 67, 67}, {1, 17, 4, 76, 67}, {4, 1, 17, 80, 67}, {1, 4, 18, 80, 70}, {1, 4, 17, 80, 67},
+       {4, 1, 17, 80, 67}, {1, 18, 4, 80, 70}, {4, 1, 17, 80, 67}, {1, 17, 4, 76, 67}, {1, 4, 17, 67, 67}},  // Q = 4
+      {{5, 25, 1, 132, 125}, {5, 1, 25, 132, 125}, {5, 25, 1, 125, 125}, {26, 1, 5, 153, 129}, {26, 1, 5, 153, 129},
+       {5, 1, 25, 125, 125}, {5, 1, 25, 125, 125}, {5, 25, 1, 125, 125}, {5, 1, 25, 132, 125}, {5, 25, 1, 132, 125}},  // Q = 5
+      {{6, 1, 37, 221, 221}, {37, 6, 1, 224, 221}, {1, 6, 38, 228, 226}, {37, 1, 6, 228, 221}, {1, 6, 37, 228, 221},
+       {1, 6, 38, 228, 226}, {1, 39, 6, 260, 231}, {1, 6, 38, 228, 226}, {37, 6, 1, 224, 221}, {6, 1, 37, 221, 221}},  // Q = 6
+      {{1, 7, 49, 358, 343}, {52, 1, 7, 362, 361}, {7, 1, 49, 343, 343}, {1, 52, 7, 369, 361}, {1, 7, 49, 343, 343},
+       {7, 1, 49, 343, 343}, {1, 52, 7, 369, 361}, {7, 1, 49, 343, 343}, {52, 1, 7, 362, 361}, {1, 7, 49, 358, 343}},  // Q = 7
+      {{1, 71, 8, 561, 561}, {1, 65, 8, 519, 519}, {1, 8, 72, 568, 568}, {67, 1, 8, 533, 533}, {68, 1, 8, 540, 540},
+       {1, 8, 72, 568, 568}, {67, 1, 8, 533, 533}, {1, 8, 72, 568, 568}, {1, 65, 8, 519, 519}, {1, 71, 8, 561, 561}},  // Q = 8
+      {{84, 1, 9, 753, 753}, {1, 84, 9, 753, 753}, {1, 81, 9, 729, 729}, {1, 9, 81, 729, 729}, {1, 9, 81, 729, 729},
+       {1, 9, 81, 729, 729}, {1, 9, 81, 729, 729}, {1, 81, 9, 729, 729}, {1, 84, 9, 753, 753}, {84, 1, 9, 753, 753}},  // Q = 9
+      {{100, 1, 10, 1008, 1000}, {1, 113, 10, 1117, 1117}, {1, 10, 106, 1060, 1054}, {1, 113, 10, 1124, 1117},
+       {1, 10, 101, 1028, 1009}, {1, 10, 106, 1060, 1054}, {1, 113, 10, 1124, 1117}, {1, 10, 106, 1060, 1054},
+       {1, 113, 10, 1117, 1117}, {100, 1, 10, 1008, 1000}},  // Q = 10
+  };
+  return t[Q - 3][ep];
+}
+
+template <typename A, typename B>
+struct SameType {
+  static constexpr bool value = false;
+};
+template <typename A>
+struct SameType<A, A> {
+  static constexpr bool value = true;
+};
+
+template <typename T, int Q, int STAGE>
+struct TileMap {
+  static constexpr bool tuned = SameType<T, float>::value && Q >= 3 && Q <= 10 && STAGE == kStageTma;
+  __host__ __device__ static constexpr TileLay lay(int ep) {
+    return tuned ? tile_lay_f32(Q, ep) : TileLay{1, Q, tile_plane(Q), 0, tile_buf(Q)};
+  }
+  __host__ __device__ static constexpr bool same(int e1, int e2) {
+    return lay(e1).sx == lay(e2).sx && lay(e1).sy == lay(e2).sy && lay(e1).sz == lay(e2).sz && lay(e1).sg == lay(e2).sg;
+  }
+  // Values of T in one buffer region of epb teams (tuned layouts; a multiple of 4 so regions start on 16 bytes).
+  __host__ __device__ static constexpr int region(int epb) {
+    int r = 0;
+    for (int ep = 0; ep < kNumEp; ep++) {
+      const int v = (epb - 1) * lay(ep).sg + lay(ep).ext;
+      r           = v > r ? v : r;
+    }
+    return (r + 3) / 4 * 4;
+  }
+};
+
+// The three tile buffers of a team.  Tuned layouts: `base` is the block's tile area, buffer b's region starts at
+// b * bst, and the team offset comes from the epoch's layout.  Otherwise `base` is the team's first tile and buffers are
+// bst = tile_buf(Q) apart (the team stride is already in `base`).
+template <typename T, int Q, int STAGE>
+struct TileSet {
+  using Map = TileMap<T, Q, STAGE>;
+  T  *base;
+  int bst, slot;
+  __host__ __device__ static constexpr bool same(int e1, int e2) { return Map::same(e1, e2); }
+  template <int EP>
+  __device__ __forceinline__ T &at(int buf, int x, int y, int z) const {
+    constexpr TileLay L = Map::lay(EP);
+    return base[buf * bst + L.sg * slot + L.sx * x + L.sy * y + L.sz * z];
+  }
+};
+
 // Even-odd form of a J x K matrix with parity +1 (centro-symmetric) or -1 (centro-antisymmetric).
 template <typename T, int J, int K>
 struct EOMat {
@@ -269,11 +357,11 @@ struct Contract {
 
 // The element pipeline from the gathered element values to the thread's output line.  On entry either (XREG) threads
 // with a, b < P hold in xin[p] the element value at node (p, a, b), or s0[IDX(x,y,z)] holds the element values
-// (x, y, z < P) and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata component k
+// (x, y, z < P) in the layout of epoch kEpGather and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata component k
 // (kappa already applied) at point (a, b, z).  On exit, threads with a, b < P hold in out[p] the element result at node
-// (p, a, b).  Uses s0, s1, s2 (Q^3 each) and block-wide barriers.
-template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename QD, typename QW = NoWait>
-__device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P, Q> &M, int a, int b, const T (&xin)[P], QD qd, T (&out)[P],
+// (p, a, b).  Uses the three tile buffers of `tl` (each epoch in its own layout) and block-wide barriers.
+template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename TL, typename QD, typename QW = NoWait>
+__device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M, int a, int b, const T (&xin)[P], QD qd, T (&out)[P],
                                           QW qwait = QW{}) {
   using C             = Contract<T, P, Q, EO>;
   constexpr bool GRAD = QFTraits<QF>::grad;
@@ -281,20 +369,20 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
   if (a < P && b < P) {
     T in[P], o[Q];
 #pragma unroll
-    for (int k = 0; k < P; k++) in[k] = XREG ? xin[k] : s0[B200_IDX(k, a, b)];
+    for (int k = 0; k < P; k++) in[k] = XREG ? xin[k] : tl.template at<kEpGather>(0, k, a, b);
     C::interp(M, in, o);
 #pragma unroll
-    for (int j = 0; j < Q; j++) s1[B200_IDX(j, a, b)] = o[j];
+    for (int j = 0; j < Q; j++) tl.template at<kEpXY>(1, j, a, b) = o[j];
   }
   __syncthreads();
   // ---- Y interpolation: lines (x < Q, z < P) ----------------------------------------------------------------------
   if (b < P) {
     T in[P], o[Q];
 #pragma unroll
-    for (int k = 0; k < P; k++) in[k] = s1[B200_IDX(a, k, b)];
+    for (int k = 0; k < P; k++) in[k] = tl.template at<kEpXY>(1, a, k, b);
     C::interp(M, in, o);
 #pragma unroll
-    for (int j = 0; j < Q; j++) s0[B200_IDX(a, j, b)] = o[j];
+    for (int j = 0; j < Q; j++) tl.template at<kEpYZ>(0, a, j, b) = o[j];
   }
   __syncthreads();
   // ---- Z interpolation (+ Z derivative): lines (x, y) --------------------------------------------------------------
@@ -302,28 +390,28 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
   {
     T in[P];
 #pragma unroll
-    for (int k = 0; k < P; k++) in[k] = s0[B200_IDX(a, b, k)];
+    for (int k = 0; k < P; k++) in[k] = tl.template at<kEpYZ>(0, a, b, k);
     C::interp(M, in, U);
   }
   if constexpr (GRAD) {
     T dz[Q];
 #pragma unroll
-    for (int j = 0; j < Q; j++) s1[B200_IDX(a, b, j)] = U[j];
+    for (int j = 0; j < Q; j++) tl.template at<kEpU>(1, a, b, j) = U[j];
     C::grad(M, U, dz);
     __syncthreads();
     // ---- X and Y derivatives of the interpolated values ------------------------------------------------------------
     {
       T in[Q], o[Q];
 #pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(k, a, b)];
+      for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpU>(1, k, a, b);
       C::grad(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s0[B200_IDX(j, a, b)] = o[j];
+      for (int j = 0; j < Q; j++) tl.template at<kEpDX>(0, j, a, b) = o[j];
 #pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(a, k, b)];
+      for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpU>(1, a, k, b);
       C::grad(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s2[B200_IDX(a, j, b)] = o[j];
+      for (int j = 0; j < Q; j++) tl.template at<kEpDY>(2, a, j, b) = o[j];
     }
     __syncthreads();
     // ---- pointwise QFunction on the z-line (x = a, y = b) ------------------------------------------------------------
@@ -334,9 +422,9 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
 #pragma unroll
       for (int k = 0; k < 6; k++) D[k] = qd(k, z);
       T vg[3];
-      poisson_point(D, s0[B200_IDX(a, b, z)], s2[B200_IDX(a, b, z)], dz[z], vg);
-      s0[B200_IDX(a, b, z)] = vg[0];
-      s2[B200_IDX(a, b, z)] = vg[1];
+      poisson_point(D, tl.template at<kEpDX>(0, a, b, z), tl.template at<kEpDY>(2, a, b, z), dz[z], vg);
+      tl.template at<kEpDX>(0, a, b, z) = vg[0];
+      tl.template at<kEpDY>(2, a, b, z) = vg[1];
       dz[z]                 = vg[2];
     }
     __syncthreads();
@@ -344,20 +432,20 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
     {
       T in[Q], o[Q];
 #pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s0[B200_IDX(k, a, b)];
+      for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpDX>(0, k, a, b);
       C::grad_t(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s1[B200_IDX(j, a, b)] = o[j];
+      for (int j = 0; j < Q; j++) tl.template at<kEpT>(1, j, a, b) = o[j];
     }
     __syncthreads();
     // ---- Y derivative, transposed, accumulated: lines (x, z) ---------------------------------------------------------
     {
       T in[Q], o[Q];
 #pragma unroll
-      for (int k = 0; k < Q; k++) in[k] = s2[B200_IDX(a, k, b)];
+      for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpDY>(2, a, k, b);
       C::grad_t(M, in, o);
 #pragma unroll
-      for (int j = 0; j < Q; j++) s1[B200_IDX(a, j, b)] += o[j];
+      for (int j = 0; j < Q; j++) tl.template at<kEpT>(1, a, j, b) += o[j];
     }
     __syncthreads();
     // ---- Z derivative transposed + sum, then Z interpolation transposed: lines (x, y) --------------------------------
@@ -365,38 +453,40 @@ __device__ __forceinline__ void op_stages(T *s0, T *s1, T *s2, const OpMats<T, P
       T w[Q], o[P];
       C::grad_t(M, dz, w);
 #pragma unroll
-      for (int j = 0; j < Q; j++) w[j] += s1[B200_IDX(a, b, j)];
+      for (int j = 0; j < Q; j++) w[j] += tl.template at<kEpT>(1, a, b, j);
       C::interp_t(M, w, o);
 #pragma unroll
-      for (int p = 0; p < P; p++) s0[B200_IDX(a, b, p)] = o[p];
+      for (int p = 0; p < P; p++) tl.template at<kEpZT>(0, a, b, p) = o[p];
     }
   } else {
     // ---- mass: pointwise product on the z-line, then Z interpolation transposed ----------------------------------------
-    // Each thread reads and rewrites only its own z-line of s0, so no barrier is needed here.
+    // With one layout for both epochs each thread reads and rewrites only its own z-line of buffer 0, so no barrier is
+    // needed here; otherwise the Z interpolation's reads must finish first.
     T w[Q], o[P];
     qwait();
 #pragma unroll
     for (int z = 0; z < Q; z++) w[z] = U[z] * qd(0, z);
     C::interp_t(M, w, o);
+    if constexpr (!TL::same(kEpYZ, kEpZT)) __syncthreads();
 #pragma unroll
-    for (int p = 0; p < P; p++) s0[B200_IDX(a, b, p)] = o[p];
+    for (int p = 0; p < P; p++) tl.template at<kEpZT>(0, a, b, p) = o[p];
   }
   __syncthreads();
   // ---- Y interpolation transposed: lines (x < Q, z < P) ----------------------------------------------------------------
   if (b < P) {
     T in[Q], o[P];
 #pragma unroll
-    for (int k = 0; k < Q; k++) in[k] = s0[B200_IDX(a, k, b)];
+    for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpZT>(0, a, k, b);
     C::interp_t(M, in, o);
 #pragma unroll
-    for (int p = 0; p < P; p++) s1[B200_IDX(a, p, b)] = o[p];
+    for (int p = 0; p < P; p++) tl.template at<kEpYT>(1, a, p, b) = o[p];
   }
   __syncthreads();
   // ---- X interpolation transposed: lines (y, z) < P --------------------------------------------------------------------
   if (a < P && b < P) {
     T in[Q];
 #pragma unroll
-    for (int k = 0; k < Q; k++) in[k] = s1[B200_IDX(k, a, b)];
+    for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpYT>(1, k, a, b);
     C::interp_t(M, in, out);
   }
 }
@@ -434,7 +524,10 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   // Bulk-copy staging: [mbarrier][NQK slabs][team tiles]; the other stagings start with the team tiles.
   const size_t       prefix = STAGE == kStageTma ? tma_prefix_bytes<S, Q, NQK>(args.epb) : 0;
   unsigned long long *bar   = reinterpret_cast<unsigned long long *>(smem_raw);
-  T *s0 = reinterpret_cast<T *>(smem_raw + prefix) + slot * SH::team_smem, *s1 = s0 + tile_buf(Q), *s2 = s1 + tile_buf(Q), *sq = s2 + tile_buf(Q);
+  using TM          = TileMap<T, Q, STAGE>;
+  T *const tiles    = reinterpret_cast<T *>(smem_raw + prefix);
+  T *s0 = tiles + (TM::tuned ? 0 : slot * SH::team_smem), *sq = s0 + 3 * tile_buf(Q);  // sq: shared-memory qdata staging
+  const TileSet<T, Q, STAGE> tl{s0, TM::tuned ? TM::region(args.epb) : tile_buf(Q), slot};
 
   // ---- qdata staging ------------------------------------------------------------------------------------------------
   // Register staging keeps the loaded storage values (S) and converts at first use, so that the loads stay in flight
@@ -560,15 +653,15 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
 #pragma unroll
       for (int r = 0; r < PU; r++) {
         const int i = tid + r * Q2;
-        if (i < P3) s0[B200_IDX(i % P, (i / P) % P, i / (P * P))] = active ? T(args.u[(int64_t)off_line[r] + c * args.comp_stride]) : T(0);
+        if (i < P3) tl.template at<kEpGather>(0, i % P, (i / P) % P, i / (P * P)) = active ? T(args.u[(int64_t)off_line[r] + c * args.comp_stride]) : T(0);
       }
       __syncthreads();
-      if (c == 0) op_stages<T, P, Q, QF, EO, false>(s0, s1, s2, M, a, b, xin, qd, out, qwait);
-      else op_stages<T, P, Q, QF, EO, false>(s0, s1, s2, M, a, b, xin, qd, out);
-      // s0 was last read by the Y interpolation (transposed), before the barrier that preceded the X stage.
+      if (c == 0) op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, xin, qd, out, qwait);
+      else op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, xin, qd, out);
+      // Buffer 0 was last read by the Y interpolation (transposed), before the barrier that preceded the X stage.
       if (owner) {
 #pragma unroll
-        for (int p = 0; p < P; p++) s0[B200_IDX(p, a, b)] = out[p];
+        for (int p = 0; p < P; p++) tl.template at<kEpScatter>(0, p, a, b) = out[p];
       }
       __syncthreads();
       if (active) {
@@ -577,7 +670,7 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
         for (int r = 0; r < PU; r++) {
           const int i = tid + r * Q2;
           if (i < P3) {
-            const T val = s0[B200_IDX(i % P, (i / P) % P, i / (P * P))];
+            const T val = tl.template at<kEpScatter>(0, i % P, (i / P) % P, i / (P * P));
             if (args.det) args.e_out[((int64_t)c * ne + e) * P3 + i] = (S)val;
             else atomicAdd(&args.v[(int64_t)off_line[r] + c * args.comp_stride], (S)val);
           }
@@ -586,8 +679,8 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     } else {
 #pragma unroll
       for (int p = 0; p < P; p++) xin[p] = (owner && active) ? T(args.u[(int64_t)off_line[p] + c * args.comp_stride]) : T(0);
-      if (c == 0) op_stages<T, P, Q, QF, EO, true>(s0, s1, s2, M, a, b, xin, qd, out, qwait);
-      else op_stages<T, P, Q, QF, EO, true>(s0, s1, s2, M, a, b, xin, qd, out);
+      if (c == 0) op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, xin, qd, out, qwait);
+      else op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, xin, qd, out);
       if (owner && active) scatter_line<T, P>(args, e, c, off_line, a, b, out);
     }
   }
@@ -692,7 +785,7 @@ __global__ void k_op_apply_pipe(const OpArgs<typename Store<T>::type> args, cons
       else return sq[k * Q3 + q];
     };
     T out[P], none[P];
-    op_stages<T, P, Q, QF, true, false>(s0, s1, s2, M, a, b, none, qd, out);
+    op_stages<T, P, Q, QF, true, false>(TileSet<T, Q, kStagePipe>{s0, tile_buf(Q), slot}, M, a, b, none, qd, out);
     if (a < P && b < P && active) scatter_line<T, P>(args, e, 0, soff + P * (a + P * b), a, b, out);
     buf ^= 1;
   }

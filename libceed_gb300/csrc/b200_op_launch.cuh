@@ -95,6 +95,7 @@ size_t op_smem(int epb) {
   constexpr int Q = P + 1;
   size_t        prefix = 0;
   if constexpr (STAGE == kStageTma) prefix = tma_prefix_bytes<typename Store<T>::type, Q, QFTraits<QF>::nqk>(epb);
+  if constexpr (TileMap<T, Q, STAGE>::tuned) return prefix + sizeof(T) * 3 * (size_t)TileMap<T, Q, STAGE>::region(epb);
   return prefix + sizeof(T) * (size_t)epb * OpShape<T, P, Q, QF, STAGE>::team_smem;
 }
 
