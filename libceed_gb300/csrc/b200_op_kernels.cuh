@@ -29,6 +29,7 @@
 //                              contiguous range: one thread issues one cp.async.bulk per component at entry, completing
 //                              on an mbarrier that the threads wait on (bounded) just before the pointwise stage, so the
 //                              copy overlaps the gather and the interpolation without registers or load instructions.
+//   k_op_apply<.., kStageLate> nothing staged: the pointwise stage loads each point's qdata from global memory.
 //   k_op_apply_3d              "point" mapping: a team of Q^3 threads per element, one thread per output point of
 //                              each stage (Q*P*P, Q*Q*P, Q^3, ... threads active), the 1D matrices in shared memory
 //                              and the thread's own qdata in registers (one coalesced load per component).
@@ -44,7 +45,9 @@
 namespace b200 {
 
 // kStage3D: point mapping (k_op_apply_3d); kStageTma: the block's qdata slabs arrive by bulk copy (TMA engine)
-enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4, kStageTma = 5 };
+// kStageLate: nothing is staged; the pointwise stage reads each point's qdata from global memory when it needs it, so the
+// kernel holds neither the qdata registers of kStageReg nor the slabs of kStageTma (higher occupancy where those limit it)
+enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4, kStageTma = 5, kStageLate = 6 };
 
 // Shared-memory layout of an element tile: point (x, y, z) at x + Q*y + tile_plane(Q)*z, three tiles per team
 // (tile_buf each), and a team stride that is fixed modulo 32 words.  The plane padding and the team stride residue
@@ -610,7 +613,12 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
     }
   };
   auto qd = [&](int k, int z) -> T {
-    if constexpr (STAGE == kStageReg) {
+    if constexpr (STAGE == kStageLate) {
+      const int64_t q = e * Q3 + B200_QLIN(a, b, z);
+      if (!active) return T(0);
+      if constexpr (TR::kappa) return T(args.qdata[(int64_t)k * ne * Q3 + q]) * T(args.kappa[q]);
+      else return T(args.qdata[(int64_t)k * ne * Q3 + q]);
+    } else if constexpr (STAGE == kStageReg) {
       if constexpr (KSEP) return T(rq[k][z]) * T(rk[z]);
       else return T(rq[k][z]);
     } else if constexpr (STAGE == kStageTma) {

@@ -11,7 +11,10 @@ namespace b200 {
 constexpr int kOpPMin = 2, kOpPMax = 9;  // compiled range of P_1d (Q_1d = P_1d + 1)
 
 // Kernel variants: qdata staging x contraction form.
-enum { kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kVar3D = 5, kVarTma = 6, kVarTmaEO = 7, kNumVariants = 8 };
+enum {
+  kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kVar3D = 5, kVarTma = 6, kVarTmaEO = 7, kVarLate = 8, kVarLateEO = 9,
+  kNumVariants = 10
+};
 
 // Untyped launch request; pointers are reinterpreted in the instance's precision.
 struct OpLaunch {
@@ -208,6 +211,7 @@ bool op_variant(int variant, OpInstance *out) {
     if (variant == kVarRegEO) *out = op_instance<T, P, QF, kStageReg, true>();
     else if (variant == kVarSmemEO) *out = op_instance<T, P, QF, kStageSmem, true>();
     else if (variant == kVarTmaEO) *out = op_instance<T, P, QF, kStageTma, true>();
+    else if (variant == kVarLateEO) *out = op_instance<T, P, QF, kStageLate, true>();
     else if (variant == kVar3D) *out = op_instance_3d<T, P, QF>();
     else return false;
     return true;
@@ -227,6 +231,8 @@ bool op_variant(int variant, OpInstance *out) {
       case kVar3D: *out = op_instance_3d<T, P, QF>(); return true;
       case kVarTma: *out = op_instance<T, P, QF, kStageTma, false>(); return true;
       case kVarTmaEO: *out = op_instance<T, P, QF, kStageTma, true>(); return true;
+      case kVarLate: *out = op_instance<T, P, QF, kStageLate, false>(); return true;
+      case kVarLateEO: *out = op_instance<T, P, QF, kStageLate, true>(); return true;
       default: return false;
     }
   }

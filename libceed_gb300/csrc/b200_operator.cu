@@ -157,6 +157,8 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
     *variant = kVar3D;
   } else if (stage == kStageTma) {
     *variant = eo ? kVarTmaEO : kVarTma;
+  } else if (stage == kStageLate) {
+    *variant = eo ? kVarLateEO : kVarLate;
   } else {
     B200_CHECK(false, B200_ERROR_UNSUPPORTED, "unknown qdata staging %d", stage);
   }
@@ -169,11 +171,11 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
 struct TileDefault {
   int stage, epb;
 };
-static const TileDefault kTileF64Grad[8]  = {{5, 14}, {4, 5}, {4, 1}, {4, 1}, {4, 1}, {1, 1}, {5, 3}, {5, 2}};
+static const TileDefault kTileF64Grad[8]  = {{5, 14}, {4, 5}, {4, 1}, {4, 1}, {6, 7}, {1, 1}, {6, 3}, {6, 5}};
 static const TileDefault kTileF64Mass[8]  = {{5, 14}, {1, 16}, {4, 1}, {4, 1}, {1, 6}, {1, 2}, {1, 4}, {5, 2}};
 static const TileDefault kTileF32Grad[8]  = {{5, 28}, {1, 14}, {5, 5}, {5, 3}, {5, 3}, {5, 2}, {5, 1}, {5, 2}};
 static const TileDefault kTileF32Mass[8]  = {{1, 14}, {1, 6}, {5, 5}, {5, 7}, {5, 5}, {5, 2}, {5, 2}, {5, 2}};
-static const TileDefault kTileF64XGrad[8] = {{1, 14}, {1, 20}, {1, 10}, {1, 7}, {5, 4}, {4, 1}, {5, 2}, {4, 1}};
+static const TileDefault kTileF64XGrad[8] = {{1, 14}, {1, 20}, {1, 10}, {1, 7}, {5, 4}, {6, 4}, {6, 7}, {6, 5}};
 static const TileDefault kTileF64XMass[8] = {{1, 7}, {1, 4}, {1, 5}, {1, 7}, {1, 5}, {1, 4}, {1, 3}, {1, 3}};
 static const TileDefault kTileVector[8]   = {{1, 14}, {1, 8}, {1, 7}, {1, 7}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};
 

@@ -23,7 +23,7 @@ def ceed_det():
 
 
 @pytest.mark.parametrize("case", ["poisson_n3_p4", "mass_n8_p3"])
-@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("epb", [2, 4, 5, 7])
 @pytest.mark.parametrize("family", ["f64", "f32", "f64x"])
 def test_ragged_last_block(ceed, ceed_det, case, staging, epb, family):

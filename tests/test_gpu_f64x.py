@@ -28,7 +28,7 @@ def ceed_det():
 
 @pytest.mark.parametrize("case", ["poisson_n6_p1", "poisson_n4_p2", "poisson_n3_p3", "poisson_n3_p4", "poisson_n2_p5", "poisson_n2_p6",
                                   "poisson_n2_p7", "poisson_n2_p8", "mass_n8_p3"])
-@pytest.mark.parametrize("staging", [1, 2, 4, 5])
+@pytest.mark.parametrize("staging", [1, 2, 4, 5, 6])
 @pytest.mark.parametrize("epb", [0, 3])
 def test_float_float_apply_matches_reference(ceed, ceed_det, case, staging, epb):
     for c in (ceed, ceed_det):
@@ -78,7 +78,7 @@ def test_float_float_deterministic_is_bit_reproducible(ceed_det):
 
 
 @pytest.mark.parametrize("case", ["vpoisson_n4_p2", "vpoisson_n3_p4", "vmass_n3_p4", "kappa_n3_p3"])
-@pytest.mark.parametrize("staging", [1, 2, 4, 5])
+@pytest.mark.parametrize("staging", [1, 2, 4, 5, 6])
 def test_float_float_vector_and_kappa_match_reference(ceed, ceed_det, case, staging):
     for c in (ceed, ceed_det):
         kind, box, g, objs = setup(c, case)

@@ -46,7 +46,7 @@ def test_fp64_apply_matches_reference(ceed, ceed_det, case, det):
 
 
 @pytest.mark.parametrize("case", ["poisson_n3_p4", "poisson_n6_p1", "poisson_n2_p8", "mass_n8_p3", "kappa_n3_p3", "vpoisson_n4_p2"])
-@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("epb", [1, 3])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_every_kernel_variant(ceed, ceed_det, case, staging, epb, dtype):
