@@ -68,3 +68,36 @@ def test_operator_without_elements(ceed, ceed_det, qf, det):
     v.set_value(3.0)
     op.apply_add(u, v)
     assert np.all(v.get_array_read() == 3.0)
+
+
+@pytest.mark.parametrize("staging", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("epb", [1, 3])
+@pytest.mark.parametrize("family", ["f64", "f32", "f64x"])
+def test_kappa_even_q_every_staging(ceed, staging, epb, family):
+    """kappa-weighted diffusion at degree 4 (Q = 6: every element's qdata and kappa start on 16 bytes, so the bulk-copy
+    staging copies element by element into padded slabs) against the oracle, for every staging."""
+    from libceed_gb300 import mesh
+    from libceed_gb300.smoke_case import build_poisson
+    from oracle import oracle as orc
+
+    if family == "f64x" and staging == 3:
+        pytest.skip("float-float kernels: no persistent pipelined variant")
+    dt = torch.float32 if family == "f32" else torch.float64
+    pb = orc.BoxProblem(3, 4, poisson=True, noise=0.05, seed=4104, kappa=True)
+    box = mesh.Box(3, 4, noise=0.05, seed=4104)
+    u0 = box.u()
+    ref = pb.apply(u0)
+    objs = build_poisson(ceed, box, dtype=dt, qf_name="Poisson3DApplyKappa")
+    kap = ceed.Vector(box.num_elem * box.Q ** 3, dt)
+    kap.set_array(pb.kappa)
+    op = objs["op"]
+    op.set_field("kappa", objs["rq"], None, kap)
+    op.elems_per_block, op.staging = epb, staging
+    if family == "f64x":
+        op.arithmetic = "float-float"
+    u = ceed.Vector(box.l_size, dt)
+    u.set_array(u0)
+    v = ceed.Vector(box.l_size, dt)
+    op.apply(u, v)
+    assert relinf(v.get_array_read(), ref) < (5e-5 if family == "f32" else 1e-12)
+    assert ceed.status() == 0
