@@ -225,6 +225,10 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
                "r"(bytes), "r"(smem_addr(bar))
                : "memory");
 }
+// Prefetch [src, src + bytes) from global memory into L2 (src 16-byte aligned, bytes a multiple of 16); no completion.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
 // Wait for phase `parity` of the barrier to complete, giving up after a bounded number of polls (each try_wait also
 // suspends for a bounded time).  Returns false on give-up.
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
@@ -576,6 +580,15 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   auto           comp_src = [&](int k, int64_t el) -> const S * {
     return (TR::kappa && k == NQD) ? args.kappa + el * Q3 : args.qdata + ((int64_t)k * ne + el) * Q3;
   };
+  if constexpr (STAGE == kStageLate) {
+    // Unstaged: at entry the first lanes ask the copy engine to prefetch each qdata component of the block's elements
+    // into L2 (widened to 16-byte chunks, as above), so that the pointwise stage's loads find them there.
+    if (threadIdx.x < NQK) {
+      const S     *src = comp_src(threadIdx.x, e0);
+      const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
+      bulk_prefetch_l2((const void *)lo, (unsigned)(hi - lo));
+    }
+  }
   if constexpr (STAGE == kStageTma) {
 #pragma unroll
     for (int k = 0; k < NQK; k++) qoff[k] = split ? 0 : (int)(((size_t)comp_src(k, e0) & 15) / sizeof(S));
