@@ -87,6 +87,11 @@ typedef struct {
 
 int orc_operator_apply(const orc_operator *op, const double *u, double *v, int add);
 
+/* The same apply in the blocked form of /cpu/self/opt/blocked (ceed_oracle_blocked.c): blocks of 8 elements with the
+ * element index innermost.  Requires Q >= P.  Equal to orc_operator_apply up to the order of the scatter's additions
+ * within a block. */
+int orc_operator_apply_blocked(const orc_operator *op, const double *u, double *v, int add);
+
 /* Adjoint of the kappa-weighted diffusion with respect to kappa:
  * g[e][q] = sum_ij (grad w)_i D_ij (grad u)_j at point q (w = output cotangent). */
 int orc_kappa_grad(const orc_operator *op, const double *u, const double *w, double *g);

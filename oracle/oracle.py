@@ -30,7 +30,8 @@ def build():
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "ceed_oracle.c")):
+        srcs = [os.path.join(HERE, f) for f in ("ceed_oracle.c", "ceed_oracle_blocked.c", "ceed_oracle.h")]
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
             build()
         _lib = ctypes.CDLL(LIB_PATH)
         _lib.orc_uniform.restype = ctypes.c_double
@@ -128,14 +129,17 @@ def qdata_build(n, Q, poisson, coords, quad_mode=GAUSS):
     return qd
 
 
-def operator_apply(qf, P, Q, num_comp, offsets, comp_stride, l_size, interp, grad, qdata, u, kappa=None, v=None, add=False):
+def operator_apply(qf, P, Q, num_comp, offsets, comp_stride, l_size, interp, grad, qdata, u, kappa=None, v=None, add=False,
+                   blocked=False):
+    """v = A u (add: v += A u).  blocked: the /cpu/self/opt/blocked form (ceed_oracle_blocked.c), the CPU baseline."""
     interp = np.ascontiguousarray(interp, dtype=np.float64)
     grad = np.ascontiguousarray(grad, dtype=np.float64)
     op = _OrcOperator(qf, P, Q, num_comp, offsets.size // P ** 3, comp_stride, l_size, _p(offsets), _p(interp), _p(grad),
                       _p(qdata), _p(kappa) if kappa is not None else None)
     if v is None:
         v = np.zeros(l_size)
-    assert lib().orc_operator_apply(ctypes.byref(op), _p(u), _p(v), 1 if add else 0) == 0
+    fn = lib().orc_operator_apply_blocked if blocked else lib().orc_operator_apply
+    assert fn(ctypes.byref(op), _p(u), _p(v), 1 if add else 0) == 0
     return v
 
 
@@ -176,8 +180,8 @@ class BoxProblem:
         else:
             self.qf = QF_MASS if ncomp == 1 else QF_VMASS
 
-    def apply(self, u=None, kappa=None):
+    def apply(self, u=None, kappa=None, blocked=False):
         u = self.u if u is None else u
         kap = kappa if kappa is not None else self.kappa
         return operator_apply(self.qf, self.P, self.Q, self.ncomp, self.offsets, self.comp_stride, self.l_size, self.interp,
-                              self.grad, self.qdata, np.ascontiguousarray(u), kappa=kap)
+                              self.grad, self.qdata, np.ascontiguousarray(u), kappa=kap, blocked=blocked)

@@ -7,6 +7,7 @@ small .npz files:
 
   basis.npz        1D tables (interp, grad, qref, qweight, collocated grad) for P=2..10, Q=P+1
                    Gauss, and P=Q=4 Gauss-Lobatto; standalone 3D basis applies (P=4, Q=5, 2 comps)
+  blocked.npz      v = A u of every operator case on the reference's /cpu/self/opt/blocked backend
   <case>.npz       operator cases: qdata from the gallery build QFunction, v = A u, and for a few
                    cases the restriction gather/scatter; inputs are stored as SHA-256 digests
                    (tests regenerate them with the oracle's generators and check the digest)
@@ -60,6 +61,22 @@ def main():
                 out["sha_" + key] = np.array(digest(arrays[case + "_" + key]))
         np.savez_compressed(os.path.join(HERE, case + ".npz"), **out)
     print("wrote", len(cases) + 1, "fixtures to", HERE)
+    write_blocked()
+
+
+def write_blocked():
+    """blocked.npz: v = A u of every operator case on the reference's /cpu/self/opt/blocked backend (the CPU baseline's
+    algorithm), from the same harness and inputs; needs the reference build of main()."""
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([os.path.join(ORACLE, "_ref", "ref_harness"), tmp, "/cpu/self/opt/blocked"], check=True)
+        out = {}
+        with open(os.path.join(tmp, "manifest.txt")) as f:
+            for line in f:
+                name, dtype, count = line.split()
+                if name.endswith("_v") and not name.startswith("bapply_"):
+                    out[name[:-2]] = np.fromfile(os.path.join(tmp, name + ".bin"), dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "blocked.npz"), **out)
+    print("wrote blocked.npz with", len(out), "cases")
 
 
 if __name__ == "__main__":

@@ -13,7 +13,7 @@ import pytest
 from oracle import oracle as orc
 from tests.conftest import GOLDEN, relinf
 
-CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f != "basis.npz")
+CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f not in ("basis.npz", "blocked.npz"))
 
 
 def _sha(a):
@@ -103,6 +103,25 @@ def test_operator_matches_reference(case):
         w = pb.apply() - f
         kg = orc.kappa_grad(pb.P, pb.Q, pb.offsets, pb.l_size, pb.interp, pb.grad, pb.qdata, pb.u, w)
         assert relinf(kg, g["kgrad"]) < 1e-12
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_blocked_port_matches_reference_blocked(case):
+    """The CPU baseline (the /cpu/self/opt/blocked restatement) against the reference's own opt/blocked backend on the
+    same inputs: bit-equal for the mass operators, within 1e-14 relative for diffusion (the reference computes its
+    collocated derivative matrix with its own rounding, as for the serial oracle), and within rounding of the serial
+    oracle everywhere."""
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    gb = np.load(os.path.join(GOLDEN, "blocked.npz"))
+    pb = _problem(case)
+    pb.qdata = g["qdata"]
+    if "kappa" in g:
+        pb.kappa = g["kappa"]
+    vb = pb.apply(blocked=True)
+    assert relinf(vb, gb[case]) < 1e-14
+    if case.startswith("mass") or case.startswith("vmass"):
+        assert np.array_equal(vb, gb[case])
+    assert relinf(vb, pb.apply()) < 1e-14
 
 
 def test_poisson_constant_nullspace():
