@@ -82,44 +82,59 @@ bool kgrad_lookup(int prec, int P, OpLauncher *out) {
   return prec == B200_F64 ? kgrad_table_f64(P, out) : prec == B200_F32 ? kgrad_table_f32(P, out) : false;
 }
 
-// Collocated derivative G_c = G B^+ (Q x Q), B^+ = (B^T B)^{-1} B^T by Gauss-Jordan with partial pivoting.  Same
-// matrix as CeedBasisGetCollocatedGrad (interface/ceed-basis.c:750-772), up to rounding.
+// Householder reflection A <- (I - b v v^T) A on an m x n block (row stride `row`, column stride `col`), v[0] = 1 implied.
+static void householder_reflect(double *A, const double *v, double b, int m, int n, int row, int col) {
+  for (int j = 0; j < n; j++) {
+    double w = A[j * col];
+    for (int i = 1; i < m; i++) w += v[i] * A[i * row + j * col];
+    A[j * col] -= b * w;
+    for (int i = 1; i < m; i++) A[i * row + j * col] -= b * w * v[i];
+  }
+}
+
+// Collocated derivative G_c = G B^+ (Q x Q).  B^+ is formed as CeedBasisGetCollocatedGrad forms it
+// (interface/ceed-basis.c:750-772 with CeedMatrixPseudoinverse, :1188-1300): Householder QR of B (Q x P), Q^T applied
+// to the identity, back substitution with R; then G B^+ with ascending sums.  The same operations in the same order
+// (host code built without multiply-add contraction), so G_c is bitwise the reference's table.  Returns false when B
+// is rank deficient.
 static bool collocated_grad(int P, int Q, const double *B, const double *G, double *Gc) {
-  std::vector<double> N((size_t)P * 2 * P, 0.0), pinv((size_t)P * Q, 0.0);
-  for (int i = 0; i < P; i++) {
-    for (int j = 0; j < P; j++) {
-      double s = 0.0;
-      for (int q = 0; q < Q; q++) s += B[q * P + i] * B[q * P + j];
-      N[i * 2 * P + j] = s;
+  const int           m = Q, n = P;
+  std::vector<double> a(B, B + (size_t)m * n), tau((size_t)m, 0.0), id((size_t)m * m, 0.0), v((size_t)m, 0.0), pinv((size_t)n * m, 0.0);
+  for (int i = 0; i < n && i < m - 1; i++) {
+    double sigma = 0.0;
+    v[i]         = a[i + n * i];
+    for (int j = i + 1; j < m; j++) {
+      v[j] = a[i + n * j];
+      sigma += v[j] * v[j];
     }
-    N[i * 2 * P + P + i] = 1.0;
+    const double norm = sqrt(v[i] * v[i] + sigma), r_ii = -copysign(norm, v[i]);
+    if (norm == 0.0) return false;
+    v[i] -= r_ii;
+    tau[i] = 2 * v[i] * v[i] / (v[i] * v[i] + sigma);
+    for (int j = i + 1; j < m; j++) v[j] /= v[i];
+    householder_reflect(&a[(size_t)i * n + i + 1], &v[i], tau[i], m - i, n - i - 1, n, 1);
+    a[i + n * i] = r_ii;
+    for (int j = i + 1; j < m; j++) a[i + n * j] = v[j];
   }
-  for (int c = 0; c < P; c++) {
-    int piv = c;
-    for (int r = c + 1; r < P; r++)
-      if (fabs(N[r * 2 * P + c]) > fabs(N[piv * 2 * P + c])) piv = r;
-    if (fabs(N[piv * 2 * P + c]) < 1e-300) return false;
-    if (piv != c)
-      for (int k = 0; k < 2 * P; k++) std::swap(N[c * 2 * P + k], N[piv * 2 * P + k]);
-    const double d = N[c * 2 * P + c];
-    for (int k = 0; k < 2 * P; k++) N[c * 2 * P + k] /= d;
-    for (int r = 0; r < P; r++) {
-      if (r == c) continue;
-      const double f = N[r * 2 * P + c];
-      for (int k = 0; k < 2 * P; k++) N[r * 2 * P + k] -= f * N[c * 2 * P + k];
+  for (int i = 0; i < m; i++) id[(size_t)i * m + i] = 1.0;
+  for (int i = 0; i < n; i++) {
+    for (int j = i + 1; j < m; j++) v[j] = a[(size_t)j * n + i];
+    householder_reflect(&id[(size_t)i * m], &v[i], tau[i], m - i, m, m, 1);
+  }
+  if (fabs(a[(size_t)n * n - 1]) < 1e-300) return false;
+  for (int j = 0; j < m; j++) {
+    pinv[j + m * (n - 1)] = id[j + m * (n - 1)] / a[(size_t)n * n - 1];
+    for (int i = n - 2; i >= 0; i--) {
+      pinv[j + m * i] = id[j + m * i];
+      for (int k = i + 1; k < n; k++) pinv[j + m * i] -= a[k + n * i] * pinv[j + m * k];
+      pinv[j + m * i] /= a[i + n * i];
     }
   }
-  for (int i = 0; i < P; i++)
-    for (int q = 0; q < Q; q++) {
-      double s = 0.0;
-      for (int k = 0; k < P; k++) s += N[i * 2 * P + P + k] * B[q * P + k];
-      pinv[i * Q + q] = s;
-    }
   for (int i = 0; i < Q; i++)
     for (int j = 0; j < Q; j++) {
       double s = 0.0;
-      for (int k = 0; k < P; k++) s += G[i * P + k] * pinv[k * Q + j];
-      Gc[i * Q + j] = s;
+      for (int k = 0; k < P; k++) s += G[k + i * P] * pinv[j + k * Q];
+      Gc[j + i * Q] = s;
     }
   return true;
 }

@@ -162,65 +162,82 @@ int orc_h1_lagrange_1d(int P, int Q, int quad_mode, double *interp_1d, double *g
   return 0;
 }
 
-/* Collocated derivative on the quadrature points, G * B^+ (Q x Q), as in interface/ceed-basis.c:750-772.
- * The reference forms B^+ through a Householder QR; here B^+ = (B^T B)^{-1} B^T through Gauss-Jordan with
- * partial pivoting.  Both are exact for the full-column-rank B (Q >= P); they differ only by rounding. */
-int orc_collocated_grad(int P, int Q, const double *interp_1d, const double *grad_1d, double *collo_grad_1d) {
-  double *N = (double *)calloc((size_t)(P * 2 * P), sizeof(double)); /* [B^T B | I] */
-  double *pinv = (double *)calloc((size_t)(P * Q), sizeof(double));  /* P x Q */
+/* Householder reflection A <- (I - b v v^T) A of the m x n block A (row stride `row`, column stride `col`), v[0] = 1
+ * implied; interface/ceed-basis.c:104-112. */
+static void orc_householder_reflect(double *A, const double *v, double b, int m, int n, int row, int col) {
+  for (int j = 0; j < n; j++) {
+    double w = A[j * col];
 
-  if (!N || !pinv || Q < P) {
-    free(N);
+    for (int i = 1; i < m; i++) w += v[i] * A[i * row + j * col];
+    A[j * col] -= b * w;
+    for (int i = 1; i < m; i++) A[i * row + j * col] -= b * w * v[i];
+  }
+}
+
+/* Pseudoinverse of the full-column-rank m x n (m >= n) row-major matrix `mat` into the n x m `pinv`: Householder QR,
+ * Q^T applied to the identity, back substitution with R (CeedQRFactorization, CeedHouseholderApplyQ and
+ * CeedMatrixPseudoinverse, interface/ceed-basis.c:1188-1300).  The same steps in the same order, so the tables round
+ * as the reference's do. */
+static int orc_pseudoinverse(const double *mat, int m, int n, double *pinv) {
+  double *a = (double *)malloc(sizeof(double) * (size_t)(m * n)), *tau = (double *)calloc((size_t)m, sizeof(double));
+  double *id = (double *)calloc((size_t)(m * m), sizeof(double)), *v = (double *)calloc((size_t)m, sizeof(double));
+
+  if (!a || !tau || !id || !v || n > m) {
+    free(a), free(tau), free(id), free(v);
+    return 1;
+  }
+  memcpy(a, mat, sizeof(double) * (size_t)(m * n));
+  for (int i = 0; i < n && i < m - 1; i++) {
+    double sigma = 0.0;
+
+    v[i] = a[i + n * i];
+    for (int j = i + 1; j < m; j++) {
+      v[j] = a[i + n * j];
+      sigma += v[j] * v[j];
+    }
+    const double norm = sqrt(v[i] * v[i] + sigma), r_ii = -copysign(norm, v[i]);
+
+    v[i] -= r_ii;
+    tau[i] = 2 * v[i] * v[i] / (v[i] * v[i] + sigma);
+    for (int j = i + 1; j < m; j++) v[j] /= v[i];
+    orc_householder_reflect(&a[i * n + i + 1], &v[i], tau[i], m - i, n - i - 1, n, 1);
+    a[i + n * i] = r_ii;
+    for (int j = i + 1; j < m; j++) a[i + n * j] = v[j];
+  }
+  for (int i = 0; i < m; i++) id[i * m + i] = 1.0;
+  for (int i = 0; i < n; i++) { /* Q^T id: reflectors in order */
+    for (int j = i + 1; j < m; j++) v[j] = a[j * n + i];
+    orc_householder_reflect(&id[i * m], &v[i], tau[i], m - i, m, m, 1);
+  }
+  for (int j = 0; j < m; j++) { /* pinv = R^{-1} Q^T, column by column */
+    pinv[j + m * (n - 1)] = id[j + m * (n - 1)] / a[n * n - 1];
+    for (int i = n - 2; i >= 0; i--) {
+      pinv[j + m * i] = id[j + m * i];
+      for (int k = i + 1; k < n; k++) pinv[j + m * i] -= a[k + n * i] * pinv[j + m * k];
+      pinv[j + m * i] /= a[i + n * i];
+    }
+  }
+  free(a), free(tau), free(id), free(v);
+  return 0;
+}
+
+/* Collocated derivative on the quadrature points, G * B^+ (Q x Q), as in interface/ceed-basis.c:750-772: B^+ by the
+ * Householder pseudoinverse above, then the product with the sums over k in ascending order
+ * (CeedMatrixMatrixMultiply, interface/ceed-basis.c:1163-1174). */
+int orc_collocated_grad(int P, int Q, const double *interp_1d, const double *grad_1d, double *collo_grad_1d) {
+  double *pinv = (double *)calloc((size_t)(P * Q), sizeof(double)); /* P x Q */
+
+  if (!pinv || Q < P || orc_pseudoinverse(interp_1d, Q, P, pinv)) {
     free(pinv);
     return 1;
   }
-  for (int i = 0; i < P; i++) {
-    for (int j = 0; j < P; j++) {
-      double s = 0.0;
-
-      for (int q = 0; q < Q; q++) s += interp_1d[q * P + i] * interp_1d[q * P + j];
-      N[i * 2 * P + j] = s;
-    }
-    N[i * 2 * P + P + i] = 1.0;
-  }
-  for (int c = 0; c < P; c++) {
-    int piv = c;
-
-    for (int r = c + 1; r < P; r++)
-      if (fabs(N[r * 2 * P + c]) > fabs(N[piv * 2 * P + c])) piv = r;
-    if (piv != c)
-      for (int k = 0; k < 2 * P; k++) {
-        double t = N[c * 2 * P + k];
-
-        N[c * 2 * P + k]   = N[piv * 2 * P + k];
-        N[piv * 2 * P + k] = t;
-      }
-    double d = N[c * 2 * P + c];
-
-    for (int k = 0; k < 2 * P; k++) N[c * 2 * P + k] /= d;
-    for (int r = 0; r < P; r++) {
-      if (r == c) continue;
-      double f = N[r * 2 * P + c];
-
-      for (int k = 0; k < 2 * P; k++) N[r * 2 * P + k] -= f * N[c * 2 * P + k];
-    }
-  }
-  /* pinv = (B^T B)^{-1} B^T */
-  for (int i = 0; i < P; i++)
-    for (int q = 0; q < Q; q++) {
-      double s = 0.0;
-
-      for (int k = 0; k < P; k++) s += N[i * 2 * P + P + k] * interp_1d[q * P + k];
-      pinv[i * Q + q] = s;
-    }
   for (int i = 0; i < Q; i++)
     for (int j = 0; j < Q; j++) {
       double s = 0.0;
 
-      for (int k = 0; k < P; k++) s += grad_1d[i * P + k] * pinv[k * Q + j];
-      collo_grad_1d[i * Q + j] = s;
+      for (int k = 0; k < P; k++) s += grad_1d[k + i * P] * pinv[j + k * Q];
+      collo_grad_1d[j + i * Q] = s;
     }
-  free(N);
   free(pinv);
   return 0;
 }
