@@ -140,21 +140,53 @@ struct TileMap {
   }
 };
 
-// The three tile buffers of a team.  Tuned layouts: `base` is the block's tile area, buffer b's region starts at
-// b * bst, and the team offset comes from the epoch's layout.  Otherwise `base` is the team's first tile and buffers are
-// bst = tile_buf(Q) apart (the team stride is already in `base`).
+// The three tile buffers of the block's teams.  `base` is the block's tile area.  Tuned layouts: buffer b's region
+// starts at b * bst and the team offset comes from the epoch's layout.  Otherwise a team's three tiles are bst =
+// tile_buf(Q) apart and teams `tst` apart.  at() addresses the thread's own team (slot); at_team() another one.
 template <typename T, int Q, int STAGE>
 struct TileSet {
   using Map = TileMap<T, Q, STAGE>;
   T  *base;
-  int bst, slot;
+  int bst, slot, tst;
   __host__ __device__ static constexpr bool same(int e1, int e2) { return Map::same(e1, e2); }
   template <int EP>
-  __device__ __forceinline__ T &at(int buf, int x, int y, int z) const {
+  __device__ __forceinline__ T &at_team(int buf, int x, int y, int z, int team) const {
     constexpr TileLay L = Map::lay(EP);
-    return base[buf * bst + L.sg * slot + L.sx * x + L.sy * y + L.sz * z];
+    return base[buf * bst + (Map::tuned ? L.sg : tst) * team + L.sx * x + L.sy * y + L.sz * z];
+  }
+  template <int EP>
+  __device__ __forceinline__ T &at(int buf, int x, int y, int z) const {
+    return at_team<EP>(buf, x, y, z, slot);
   }
 };
+
+// Owner of one line in the stages that work on fewer than Q^2 lines per element: the X interpolation and its transpose
+// (x-lines (y, z), y, z < P) and the Y interpolation and its transpose (y-lines (x, z), x < Q, z < P).  Packed form:
+// the block's threads take the active lines of all its teams in order (thread t of the block: team t / lines, line
+// t % lines), so whole warps are idle in these stages instead of lanes of every warp; otherwise thread (a, b) of team
+// `slot` owns line (a, b) when it is active.
+struct LineOwner {
+  int  u, w, team;  // line coordinates (y, z) for x-lines, (x, z) for y-lines
+  bool on;
+};
+template <int P, int Q, bool PACK>
+__device__ __forceinline__ LineOwner x_line_owner(int a, int b, int slot, int epb) {
+  if constexpr (PACK) {
+    const int t = threadIdx.x, team = t / (P * P), r = t % (P * P);
+    return LineOwner{r % P, r / P, team, team < epb};
+  } else {
+    return LineOwner{a, b, slot, a < P && b < P};
+  }
+}
+template <int P, int Q, bool PACK>
+__device__ __forceinline__ LineOwner y_line_owner(int a, int b, int slot, int epb) {
+  if constexpr (PACK) {
+    const int t = threadIdx.x, team = t / (Q * P), r = t % (Q * P);
+    return LineOwner{r % Q, r / Q, team, team < epb};
+  } else {
+    return LineOwner{a, b, slot, b < P};
+  }
+}
 
 // Even-odd form of a J x K matrix with parity +1 (centro-symmetric) or -1 (centro-antisymmetric).
 template <typename T, int J, int K>
@@ -362,34 +394,36 @@ struct Contract {
 #define B200_IDX(x, y, z) ((x) + Q * (y) + tile_plane(Q) * (z))  // shared-memory tile position
 #define B200_QLIN(x, y, z) ((x) + Q * ((y) + Q * (z)))         // linear point index of global arrays
 
-// The element pipeline from the gathered element values to the thread's output line.  On entry either (XREG) threads
-// with a, b < P hold in xin[p] the element value at node (p, a, b), or s0[IDX(x,y,z)] holds the element values
-// (x, y, z < P) in the layout of epoch kEpGather and every thread of the team has passed a barrier after writing it; qd(k, z) returns qdata component k
-// (kappa already applied) at point (a, b, z).  On exit, threads with a, b < P hold in out[p] the element result at node
-// (p, a, b).  Uses the three tile buffers of `tl` (each epoch in its own layout) and block-wide barriers.
+// The element pipeline from the gathered element values to the x-line owners' output lines.  Thread (a, b) of its team
+// owns z-line (a, b) in the Z stages, the derivatives and the QFunction; lx and ly name the lines it owns in the X and
+// Y stages.  On entry either (XREG) the x-line owners (lx.on) hold in xin[p] the element value at node (p, lx.u, lx.w)
+// of team lx.team, or buffer 0 holds the element values (x, y, z < P) in the layout of epoch kEpGather and every
+// thread has passed a barrier after writing them; qd(k, z) returns qdata component k (kappa already applied) at point
+// (a, b, z).  On exit the x-line owners hold in out[p] the element result at node (p, lx.u, lx.w) of team lx.team.
+// Uses the three tile buffers of `tl` (each epoch in its own layout) and block-wide barriers.
 template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename TL, typename QD, typename QW = NoWait>
-__device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M, int a, int b, const T (&xin)[P], QD qd, T (&out)[P],
-                                          QW qwait = QW{}) {
+__device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M, int a, int b, const LineOwner &lx, const LineOwner &ly,
+                                          const T (&xin)[P], QD qd, T (&out)[P], QW qwait = QW{}) {
   using C             = Contract<T, P, Q, EO>;
   constexpr bool GRAD = QFTraits<QF>::grad;
-  // ---- X interpolation: lines (y, z) < P --------------------------------------------------------------------------
-  if (a < P && b < P) {
+  // ---- X interpolation: lines (y, z) < P, owner lx ------------------------------------------------------------------
+  if (lx.on) {
     T in[P], o[Q];
 #pragma unroll
-    for (int k = 0; k < P; k++) in[k] = XREG ? xin[k] : tl.template at<kEpGather>(0, k, a, b);
+    for (int k = 0; k < P; k++) in[k] = XREG ? xin[k] : tl.template at_team<kEpGather>(0, k, lx.u, lx.w, lx.team);
     C::interp(M, in, o);
 #pragma unroll
-    for (int j = 0; j < Q; j++) tl.template at<kEpXY>(1, j, a, b) = o[j];
+    for (int j = 0; j < Q; j++) tl.template at_team<kEpXY>(1, j, lx.u, lx.w, lx.team) = o[j];
   }
   __syncthreads();
-  // ---- Y interpolation: lines (x < Q, z < P) ----------------------------------------------------------------------
-  if (b < P) {
+  // ---- Y interpolation: lines (x < Q, z < P), owner ly ------------------------------------------------------------
+  if (ly.on) {
     T in[P], o[Q];
 #pragma unroll
-    for (int k = 0; k < P; k++) in[k] = tl.template at<kEpXY>(1, a, k, b);
+    for (int k = 0; k < P; k++) in[k] = tl.template at_team<kEpXY>(1, ly.u, k, ly.w, ly.team);
     C::interp(M, in, o);
 #pragma unroll
-    for (int j = 0; j < Q; j++) tl.template at<kEpYZ>(0, a, j, b) = o[j];
+    for (int j = 0; j < Q; j++) tl.template at_team<kEpYZ>(0, ly.u, j, ly.w, ly.team) = o[j];
   }
   __syncthreads();
   // ---- Z interpolation (+ Z derivative): lines (x, y) --------------------------------------------------------------
@@ -479,21 +513,21 @@ __device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M
     for (int p = 0; p < P; p++) tl.template at<kEpZT>(0, a, b, p) = o[p];
   }
   __syncthreads();
-  // ---- Y interpolation transposed: lines (x < Q, z < P) ----------------------------------------------------------------
-  if (b < P) {
+  // ---- Y interpolation transposed: lines (x < Q, z < P), owner ly ----------------------------------------------------
+  if (ly.on) {
     T in[Q], o[P];
 #pragma unroll
-    for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpZT>(0, a, k, b);
+    for (int k = 0; k < Q; k++) in[k] = tl.template at_team<kEpZT>(0, ly.u, k, ly.w, ly.team);
     C::interp_t(M, in, o);
 #pragma unroll
-    for (int p = 0; p < P; p++) tl.template at<kEpYT>(1, a, p, b) = o[p];
+    for (int p = 0; p < P; p++) tl.template at_team<kEpYT>(1, ly.u, p, ly.w, ly.team) = o[p];
   }
   __syncthreads();
-  // ---- X interpolation transposed: lines (y, z) < P --------------------------------------------------------------------
-  if (a < P && b < P) {
+  // ---- X interpolation transposed: lines (y, z) < P, owner lx ----------------------------------------------------------
+  if (lx.on) {
     T in[Q];
 #pragma unroll
-    for (int k = 0; k < Q; k++) in[k] = tl.template at<kEpYT>(1, k, a, b);
+    for (int k = 0; k < Q; k++) in[k] = tl.template at_team<kEpYT>(1, k, lx.u, lx.w, lx.team);
     C::interp_t(M, in, out);
   }
 }
@@ -533,8 +567,8 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   unsigned long long *bar   = reinterpret_cast<unsigned long long *>(smem_raw);
   using TM          = TileMap<T, Q, STAGE>;
   T *const tiles    = reinterpret_cast<T *>(smem_raw + prefix);
-  T *s0 = tiles + (TM::tuned ? 0 : slot * SH::team_smem), *sq = s0 + 3 * tile_buf(Q);  // sq: shared-memory qdata staging
-  const TileSet<T, Q, STAGE> tl{s0, TM::tuned ? TM::region(args.epb) : tile_buf(Q), slot};
+  T *const sq       = tiles + slot * SH::team_smem + 3 * tile_buf(Q);  // shared-memory qdata staging (legacy team layout)
+  const TileSet<T, Q, STAGE> tl{tiles, TM::tuned ? TM::region(args.epb) : tile_buf(Q), slot, TM::tuned ? 0 : SH::team_smem};
 
   // ---- qdata staging ------------------------------------------------------------------------------------------------
   // Register staging keeps the loaded storage values (S) and converts at first use, so that the loads stay in flight
@@ -653,16 +687,21 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
   // kernels); the FP64 and float-float kernels, bound by their arithmetic, keep the other form: thread (a, b),
   // a, b < P, gathers and later scatters the element's x-line of nodes (p, a, b), which feeds the X interpolation from
   // registers.  Either way the thread's offsets stay in registers from the gather to the scatter.
+  // The X and Y stages take packed line owners in the kernels with the single tile layout (the per-epoch layouts were
+  // chosen for the thread (a, b) owners).
   constexpr bool CG = STAGE == kStageTma && __is_same(T, float);
+  constexpr bool PACK = !TM::tuned;
   constexpr int  PU = (P3 + Q2 - 1) / Q2;  // nodes per thread in the coalesced form
-  const bool     owner = a < P && b < P;
-  int32_t        off_line[CG ? PU : P];
+  const LineOwner lx = x_line_owner<P, Q, PACK>(a, b, slot, args.epb), ly = y_line_owner<P, Q, PACK>(a, b, slot, args.epb);
+  const int64_t   ex = e0 + lx.team;  // element of the thread's x-line
+  const bool      xact = lx.on && ex < ne;
+  int32_t         off_line[CG ? PU : P];
   if constexpr (CG) {
 #pragma unroll
     for (int r = 0; r < PU; r++) off_line[r] = (active && tid + r * Q2 < P3) ? args.offsets[e * P3 + tid + r * Q2] : 0;
   } else {
 #pragma unroll
-    for (int p = 0; p < P; p++) off_line[p] = (owner && active) ? args.offsets[e * P3 + P * (a + P * b) + p] : 0;
+    for (int p = 0; p < P; p++) off_line[p] = xact ? args.offsets[ex * P3 + P * (lx.u + P * lx.w) + p] : 0;
   }
 
   // The barrier at the top of each later component protects the tiles still being read by the previous one.
@@ -677,12 +716,12 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
         if (i < P3) tl.template at<kEpGather>(0, i % P, (i / P) % P, i / (P * P)) = active ? T(args.u[(int64_t)off_line[r] + c * args.comp_stride]) : T(0);
       }
       __syncthreads();
-      if (c == 0) op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, xin, qd, out, qwait);
-      else op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, xin, qd, out);
+      if (c == 0) op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, lx, ly, xin, qd, out, qwait);
+      else op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, lx, ly, xin, qd, out);
       // Buffer 0 was last read by the Y interpolation (transposed), before the barrier that preceded the X stage.
-      if (owner) {
+      if (lx.on) {
 #pragma unroll
-        for (int p = 0; p < P; p++) tl.template at<kEpScatter>(0, p, a, b) = out[p];
+        for (int p = 0; p < P; p++) tl.template at_team<kEpScatter>(0, p, lx.u, lx.w, lx.team) = out[p];
       }
       __syncthreads();
       if (active) {
@@ -699,10 +738,10 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
       }
     } else {
 #pragma unroll
-      for (int p = 0; p < P; p++) xin[p] = (owner && active) ? T(args.u[(int64_t)off_line[p] + c * args.comp_stride]) : T(0);
-      if (c == 0) op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, xin, qd, out, qwait);
-      else op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, xin, qd, out);
-      if (owner && active) scatter_line<T, P>(args, e, c, off_line, a, b, out);
+      for (int p = 0; p < P; p++) xin[p] = xact ? T(args.u[(int64_t)off_line[p] + c * args.comp_stride]) : T(0);
+      if (c == 0) op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, lx, ly, xin, qd, out, qwait);
+      else op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, lx, ly, xin, qd, out);
+      if (xact) scatter_line<T, P>(args, ex, c, off_line, lx.u, lx.w, out);
     }
   }
 }
@@ -806,7 +845,9 @@ __global__ void k_op_apply_pipe(const OpArgs<typename Store<T>::type> args, cons
       else return sq[k * Q3 + q];
     };
     T out[P], none[P];
-    op_stages<T, P, Q, QF, true, false>(TileSet<T, Q, kStagePipe>{s0, tile_buf(Q), slot}, M, a, b, none, qd, out);
+    const LineOwner lx = x_line_owner<P, Q, false>(a, b, slot, args.epb), ly = y_line_owner<P, Q, false>(a, b, slot, args.epb);
+    op_stages<T, P, Q, QF, true, false>(TileSet<T, Q, kStagePipe>{reinterpret_cast<T *>(smem_raw), tile_buf(Q), slot, SH::team_smem}, M, a, b, lx, ly,
+                                        none, qd, out);
     if (a < P && b < P && active) scatter_line<T, P>(args, e, 0, soff + P * (a + P * b), a, b, out);
     buf ^= 1;
   }
