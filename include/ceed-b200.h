@@ -280,6 +280,12 @@ int b200_fma_peak(b200_ctx ctx, int prec, double *tflops);
  *      so moving contractions of the FP64 kernels onto the tensor path cannot raise their bound.  Blocks the host. */
 int b200_fp64_tensor_peak(b200_ctx ctx, double *dmma_tflops, double *mixed_tflops);
 
+/* ---- Bounded-wait self-test.  No counterpart in the reference: one block waits, with the bounded mbarrier wait of the
+ *      bulk-copy kernels and at most max_polls polls (1..65536), on a barrier that nothing completes, and records the
+ *      give-up in the context's status word (B200_STATUS_COPY_TIMEOUT, read with b200_ctx_status), so that this path
+ *      is exercised without a fault; the context stays usable.  Blocks the host. */
+int b200_wait_selftest(b200_ctx ctx, int max_polls);
+
 #ifdef __cplusplus
 }
 #endif

@@ -263,8 +263,8 @@ __device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes
 }
 // Wait for phase `parity` of the barrier to complete, giving up after a bounded number of polls (each try_wait also
 // suspends for a bounded time).  Returns false on give-up.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-  for (int i = 0; i < (1 << 22); i++) {
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int max_polls = 1 << 22) {
+  for (int i = 0; i < max_polls; i++) {
     unsigned done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

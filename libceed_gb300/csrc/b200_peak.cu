@@ -1,5 +1,6 @@
 // FMA-rate probe (b200_fma_peak): the denominator of the compute roofline of the fused FP64 and FP32 kernels.
 #include "b200_internal.cuh"
+#include "b200_op_kernels.cuh"
 
 namespace b200 {
 
@@ -113,9 +114,29 @@ static int dmma_peak(b200_ctx ctx, int iters, double *dmma_tflops, double *mixed
   return B200_SUCCESS;
 }
 
+// Give-up path of the bounded mbarrier wait: every thread of one block waits, with the wait of the bulk-copy kernels and
+// a bound of max_polls, on a barrier whose phase nothing completes (no copy is issued and no thread arrives), then the
+// first thread records the give-up in the context's status word, as the kernels do.
+__global__ void k_wait_selftest(int *status, int max_polls) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  const bool done = mbar_wait(&bar, 0, max_polls);
+  __syncthreads();
+  if (!done && threadIdx.x == 0) atomicOr(status, B200_STATUS_COPY_TIMEOUT);
+}
+
 }  // namespace b200
 
 using namespace b200;
+
+extern "C" int b200_wait_selftest(b200_ctx ctx, int max_polls) {
+  B200_CHECK(max_polls >= 1 && max_polls <= (1 << 16), B200_ERROR_DIMENSION, "b200_wait_selftest: max_polls must be in [1, 65536]");
+  k_wait_selftest<<<1, 64, 0, ctx->stream>>>(ctx->d_status, max_polls);
+  B200_LAUNCHED(ctx, "wait_selftest");
+  B200_CUDA(cudaStreamSynchronize(ctx->stream));
+  return B200_SUCCESS;
+}
 
 extern "C" int b200_fp64_tensor_peak(b200_ctx ctx, double *dmma_tflops, double *mixed_tflops) {
   B200_CHECK(dmma_tflops && mixed_tflops, B200_ERROR_INCOMPLETE, "b200_fp64_tensor_peak: both outputs are required");

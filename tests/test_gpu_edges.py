@@ -101,3 +101,21 @@ def test_kappa_even_q_every_staging(ceed, staging, epb, family):
     op.apply(u, v)
     assert relinf(v.get_array_read(), ref) < (5e-5 if family == "f32" else 1e-12)
     assert ceed.status() == 0
+
+
+def test_bounded_wait_gives_up_and_context_survives(ceed):
+    """A bounded mbarrier wait that nothing completes gives up, sets the status bit the host reads, and leaves the
+    context usable: the next apply still matches the reference."""
+    from libceed_gb300._ffi import call
+
+    ceed.status()
+    call("b200_wait_selftest", ceed._ctx, 256)
+    assert ceed.status() == 1  # B200_STATUS_COPY_TIMEOUT, cleared by the read
+    assert ceed.status() == 0
+    kind, box, g, objs = setup(ceed, "poisson_n3_p4")
+    u = ceed.Vector(box.l_size)
+    u.set_array(box.u())
+    v = ceed.Vector(box.l_size)
+    objs["op"].apply(u, v)
+    assert relinf(v.get_array_read(), g["v"]) < 1e-12
+    assert ceed.status() == 0
