@@ -164,7 +164,8 @@ typedef struct {
   int            elems_per_block; /* 0: tuned default */
   int            staging;         /* 0: default, 1: registers, 2: shared memory, 3: persistent pipelined,
                                      4: point (Q^3-thread) mapping, 5: bulk-copy (TMA) qdata slabs,
-                                     6: none (qdata read from global memory in the pointwise stage) */
+                                     6: none (qdata read from global memory in the pointwise stage),
+                                     7: persistent blocks with bulk-copy staging one batch ahead (FP32, one component) */
 } b200_op_desc;
 
 int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);

@@ -47,7 +47,8 @@ namespace b200 {
 // kStage3D: point mapping (k_op_apply_3d); kStageTma: the block's qdata slabs arrive by bulk copy (TMA engine)
 // kStageLate: nothing is staged; the pointwise stage reads each point's qdata from global memory when it needs it, so the
 // kernel holds neither the qdata registers of kStageReg nor the slabs of kStageTma (higher occupancy where those limit it)
-enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4, kStageTma = 5, kStageLate = 6 };
+// kStagePTma: persistent blocks over element batches, bulk-copy staging one batch ahead (FP32, one component)
+enum { kStageReg = 1, kStageSmem = 2, kStagePipe = 3, kStage3D = 4, kStageTma = 5, kStageLate = 6, kStagePTma = 7 };
 
 // Shared-memory layout of an element tile: point (x, y, z) at x + Q*y + tile_plane(Q)*z, three tiles per team
 // (tile_buf each), and a team stride that is fixed modulo 32 words.  The plane padding and the team stride residue
@@ -399,11 +400,12 @@ struct Contract {
 // Y stages.  On entry either (XREG) the x-line owners (lx.on) hold in xin[p] the element value at node (p, lx.u, lx.w)
 // of team lx.team, or buffer 0 holds the element values (x, y, z < P) in the layout of epoch kEpGather and every
 // thread has passed a barrier after writing them; qd(k, z) returns qdata component k (kappa already applied) at point
-// (a, b, z).  On exit the x-line owners hold in out[p] the element result at node (p, lx.u, lx.w) of team lx.team.
-// Uses the three tile buffers of `tl` (each epoch in its own layout) and block-wide barriers.
-template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename TL, typename QD, typename QW = NoWait>
+// (a, b, z), after qwait() has returned; qafter() runs once all threads are past their last qdata read.  On exit the
+// x-line owners hold in out[p] the element result at node (p, lx.u, lx.w) of team lx.team.  Uses the three tile buffers
+// of `tl` (each epoch in its own layout) and block-wide barriers.
+template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename TL, typename QD, typename QW = NoWait, typename QA = NoWait>
 __device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M, int a, int b, const LineOwner &lx, const LineOwner &ly,
-                                          const T (&xin)[P], QD qd, T (&out)[P], QW qwait = QW{}) {
+                                          const T (&xin)[P], QD qd, T (&out)[P], QW qwait = QW{}, QA qafter = QA{}) {
   using C             = Contract<T, P, Q, EO>;
   constexpr bool GRAD = QFTraits<QF>::grad;
   // ---- X interpolation: lines (y, z) < P, owner lx ------------------------------------------------------------------
@@ -513,6 +515,7 @@ __device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M
     for (int p = 0; p < P; p++) tl.template at<kEpZT>(0, a, b, p) = o[p];
   }
   __syncthreads();
+  qafter();  // every thread is past its last qdata read
   // ---- Y interpolation transposed: lines (x < Q, z < P), owner ly ----------------------------------------------------
   if (ly.on) {
     T in[Q], o[P];
@@ -742,6 +745,148 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
       if (c == 0) op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, lx, ly, xin, qd, out, qwait);
       else op_stages<T, P, Q, QF, EO, true>(tl, M, a, b, lx, ly, xin, qd, out);
       if (xact) scatter_line<T, P>(args, ex, c, off_line, lx.u, lx.w, out);
+    }
+  }
+}
+
+// Persistent form of the FP32 bulk-copy kernel (one component).  Block i handles element batches i, i + gridDim.x, ...
+// with the same stages, layouts and coalesced gather and scatter as k_op_apply<float, ..., kStageTma>, and works one
+// batch ahead: while batch j is computed, the values of batch j + 1 are loaded into registers (their offsets were loaded
+// one batch earlier still), and once every thread is past its last qdata read of batch j the bulk copies of batch j + 1's
+// qdata are issued into the same slabs, completing on the same mbarrier (phase parity alternating with the batch count).
+// Every copy issued is waited for, so none is in flight when a block exits.
+template <typename T, int P, int Q, int QF, bool EO>
+__global__ void k_op_apply_ptma(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
+  static_assert(SameType<T, float>::value && QFTraits<QF>::nc == 1, "the persistent bulk-copy kernel is FP32, one component");
+  using TR         = QFTraits<QF>;
+  using TM         = TileMap<T, Q, kStageTma>;
+  constexpr int Q2 = Q * Q, Q3 = Q * Q * Q, P3 = P * P * P, NQD = TR::nqd, NQK = TR::nqk;
+  constexpr int PU = (P3 + Q2 - 1) / Q2;  // nodes per thread in the coalesced gather and scatter
+  using S          = T;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int     tid = threadIdx.x % Q2, slot = threadIdx.x / Q2;
+  const int     a = tid % Q, b = tid / Q;
+  const int64_t ne     = args.num_elem;
+  const int64_t nbatch = (ne + args.epb - 1) / args.epb;
+  const size_t  prefix = tma_prefix_bytes<S, Q, NQK>(args.epb);
+  const size_t  slab   = tma_slab_bytes<S, Q>(args.epb);
+  constexpr int SQ     = tma_elem_stride<S, Q>();
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw);
+  T *const             tiles = reinterpret_cast<T *>(smem_raw + prefix);
+  const TileSet<T, Q, kStageTma> tl{tiles, TM::region(args.epb), slot, 0};
+  const LineOwner lx = x_line_owner<P, Q, false>(a, b, slot, args.epb), ly = y_line_owner<P, Q, false>(a, b, slot, args.epb);
+  const bool      split = (Q3 * sizeof(S)) % 16 == 0 && (((size_t)args.qdata | (size_t)args.kappa) & 15) == 0;
+  const int       estr  = split ? SQ : Q3;
+  auto comp_src = [&](int k, int64_t el) -> const S * {
+    return (TR::kappa && k == NQD) ? args.kappa + el * Q3 : args.qdata + ((int64_t)k * ne + el) * Q3;
+  };
+  // Bulk copies of one batch's qdata (warp 0; lane 0 arms the barrier for the batch's bytes first).
+  auto issue = [&](int64_t batch) {
+    if (threadIdx.x >= 32) return;
+    // The slabs were last read by the threads (generic proxy) before a barrier; order those reads before the copy
+    // engine's writes (async proxy).
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    const int64_t e0 = batch * args.epb;
+    const int     nb = (int)((ne - e0) < args.epb ? (ne - e0) : args.epb);
+    if (split) {
+      if (threadIdx.x == 0) mbar_arrive_expect_tx(bar, (unsigned)(NQK * nb * Q3 * sizeof(S)));
+      __syncwarp();
+      for (int i = threadIdx.x; i < NQK * nb; i += 32) {
+        const int k = i / nb, el = i % nb;
+        bulk_copy_g2s(smem_raw + 16 + k * slab + (size_t)el * SQ * sizeof(S), comp_src(k, e0 + el), (unsigned)(Q3 * sizeof(S)), bar);
+      }
+    } else if (threadIdx.x == 0) {
+      unsigned total = 0;
+      for (int k = 0; k < NQK; k++) {
+        const S     *src = comp_src(k, e0);
+        const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
+        total += (unsigned)(hi - lo);
+      }
+      mbar_arrive_expect_tx(bar, total);
+      for (int k = 0; k < NQK; k++) {
+        const S     *src = comp_src(k, e0);
+        const size_t lo = (size_t)src & ~(size_t)15, hi = ((size_t)(src + (size_t)nb * Q3) + 15) & ~(size_t)15;
+        bulk_copy_g2s(smem_raw + 16 + k * slab, (const void *)lo, (unsigned)(hi - lo), bar);
+      }
+    }
+  };
+  auto load_offsets = [&](int64_t batch, int32_t (&o)[PU]) {
+    const int64_t e = batch * args.epb + slot;
+#pragma unroll
+    for (int r = 0; r < PU; r++) o[r] = (batch < nbatch && e < ne && tid + r * Q2 < P3) ? args.offsets[e * P3 + tid + r * Q2] : 0;
+  };
+  auto load_u = [&](int64_t batch, const int32_t (&o)[PU], T (&uv)[PU]) {
+    const int64_t e = batch * args.epb + slot;
+#pragma unroll
+    for (int r = 0; r < PU; r++) uv[r] = (batch < nbatch && e < ne && tid + r * Q2 < P3) ? args.u[o[r]] : T(0);
+  };
+
+  int64_t batch = blockIdx.x;
+  if (batch >= nbatch) return;
+  if (threadIdx.x == 0) mbar_init(bar, 1);
+  __syncthreads();
+  issue(batch);
+  int32_t o_cur[PU], o_nxt[PU], o_nn[PU];
+  T       u_cur[PU], u_nxt[PU];
+  load_offsets(batch, o_cur);
+  load_u(batch, o_cur, u_cur);
+  load_offsets(batch + gridDim.x, o_nxt);
+  unsigned parity = 0;
+#pragma unroll 1
+  for (; batch < nbatch; batch += gridDim.x, parity ^= 1) {
+    const int64_t e0 = batch * args.epb, e = e0 + slot;
+    const bool    active = e < ne;
+    const int64_t next = batch + gridDim.x;
+    __syncthreads();  // the previous batch's scatter reads of buffer 0 are done
+#pragma unroll
+    for (int r = 0; r < PU; r++) {
+      const int i = tid + r * Q2;
+      if (i < P3) tl.template at<kEpGather>(0, i % P, (i / P) % P, i / (P * P)) = u_cur[r];
+    }
+    // The next batch's values and the offsets of the one after: in flight while this batch is computed.
+    load_u(next, o_nxt, u_nxt);
+    load_offsets(next + gridDim.x, o_nn);
+    __syncthreads();
+    int qoff[NQK];
+#pragma unroll
+    for (int k = 0; k < NQK; k++) qoff[k] = split ? 0 : (int)(((size_t)comp_src(k, e0) & 15) / sizeof(S));
+    auto qwait = [&]() {
+      if (!mbar_wait(bar, parity) && threadIdx.x == 0) atomicOr(args.status, B200_STATUS_COPY_TIMEOUT);
+    };
+    auto qafter = [&]() {
+      if (next < nbatch) issue(next);
+    };
+    auto qd = [&](int k, int z) -> T {
+      const S  *sl = reinterpret_cast<const S *>(smem_raw + 16);
+      const int q  = slot * estr + B200_QLIN(a, b, z);
+      const int st = (int)(slab / sizeof(S));
+      if constexpr (TR::kappa) return T(sl[k * st + qoff[k] + q]) * T(sl[NQD * st + qoff[NQD] + q]);
+      else return T(sl[k * st + qoff[k] + q]);
+    };
+    T none[P], out[P];
+    op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, lx, ly, none, qd, out, qwait, qafter);
+    // Buffer 0 was last read by the Y interpolation (transposed), before the barrier that preceded the X stage.
+    if (lx.on) {
+#pragma unroll
+      for (int p = 0; p < P; p++) tl.template at_team<kEpScatter>(0, p, lx.u, lx.w, lx.team) = out[p];
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int r = 0; r < PU; r++) {
+        const int i = tid + r * Q2;
+        if (i < P3) {
+          const T val = tl.template at<kEpScatter>(0, i % P, (i / P) % P, i / (P * P));
+          if (args.det) args.e_out[e * P3 + i] = (S)val;
+          else atomicAdd(&args.v[o_cur[r]], (S)val);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < PU; r++) {
+      o_cur[r] = o_nxt[r];
+      o_nxt[r] = o_nn[r];
+      u_cur[r] = u_nxt[r];
     }
   }
 }

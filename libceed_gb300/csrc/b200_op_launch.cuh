@@ -13,7 +13,7 @@ constexpr int kOpPMin = 2, kOpPMax = 9;  // compiled range of P_1d (Q_1d = P_1d 
 // Kernel variants: qdata staging x contraction form.
 enum {
   kVarReg = 0, kVarSmem = 1, kVarRegEO = 2, kVarSmemEO = 3, kVarPipeEO = 4, kVar3D = 5, kVarTma = 6, kVarTmaEO = 7, kVarLate = 8, kVarLateEO = 9,
-  kNumVariants = 10
+  kVarPTma = 10, kVarPTmaEO = 11, kNumVariants = 12
 };
 
 // Untyped launch request; pointers are reinterpreted in the instance's precision.
@@ -204,6 +204,33 @@ OpInstance op_instance_pipe() {
   return inst;
 }
 
+template <typename T, int P, int QF, bool EO>
+int op_launch_ptma(b200_ctx ctx, const OpLaunch &r) {
+  constexpr int Q    = P + 1;
+  auto          kern = k_op_apply_ptma<T, P, Q, QF, EO>;
+  const size_t  smem = op_smem<T, P, QF, kStageTma>(r.epb);
+  if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t nbatch = ceil_div(r.num_elem, r.epb);
+  const int64_t grid   = r.grid < nbatch ? r.grid : nbatch;
+  if (grid <= 0) return B200_SUCCESS;
+  kern<<<(unsigned)grid, r.epb * Q * Q, smem, ctx->stream>>>(make_args<T>(r), make_mats<T, P, Q>(r.B, r.G));
+  B200_LAUNCHED(ctx, "op_apply_ptma");
+  return B200_SUCCESS;
+}
+
+template <typename T, int P, int QF, bool EO>
+int op_occupancy_ptma(int epb) {
+  return blocks_per_sm(k_op_apply_ptma<T, P, P + 1, QF, EO>, epb * (P + 1) * (P + 1), op_smem<T, P, QF, kStageTma>(epb));
+}
+
+template <typename T, int P, int QF, bool EO>
+OpInstance op_instance_ptma() {
+  OpInstance         inst{op_launch_ptma<T, P, QF, EO>, op_smem<T, P, QF, kStageTma>, op_occupancy_ptma<T, P, QF, EO>, 1024, true};
+  cudaFuncAttributes attr;
+  if (cudaFuncGetAttributes(&attr, k_op_apply_ptma<T, P, P + 1, QF, EO>) == cudaSuccess) inst.max_threads = attr.maxThreadsPerBlock;
+  return inst;
+}
+
 template <typename T, int P, int QF>
 bool op_variant(int variant, OpInstance *out) {
   if constexpr (__is_same(T, dfloat)) {
@@ -233,6 +260,14 @@ bool op_variant(int variant, OpInstance *out) {
       case kVarTmaEO: *out = op_instance<T, P, QF, kStageTma, true>(); return true;
       case kVarLate: *out = op_instance<T, P, QF, kStageLate, false>(); return true;
       case kVarLateEO: *out = op_instance<T, P, QF, kStageLate, true>(); return true;
+      case kVarPTma:
+      case kVarPTmaEO:
+        if constexpr (__is_same(T, float) && QFTraits<QF>::nc == 1) {
+          *out = variant == kVarPTma ? op_instance_ptma<T, P, QF, false>() : op_instance_ptma<T, P, QF, true>();
+          return true;
+        } else {
+          return false;
+        }
       default: return false;
     }
   }

@@ -174,6 +174,10 @@ static int op_variant_of(b200_op op, int stage, int *variant) {
     *variant = eo ? kVarTmaEO : kVarTma;
   } else if (stage == kStageLate) {
     *variant = eo ? kVarLateEO : kVarLate;
+  } else if (stage == kStagePTma) {
+    B200_CHECK(op->d.prec == B200_F32 && op->d.num_comp == 1, B200_ERROR_UNSUPPORTED,
+               "the persistent bulk-copy kernel is FP32 with one component");
+    *variant = eo ? kVarPTmaEO : kVarPTma;
   } else {
     B200_CHECK(false, B200_ERROR_UNSUPPORTED, "unknown qdata staging %d", stage);
   }
@@ -188,8 +192,8 @@ struct TileDefault {
 };
 static const TileDefault kTileF64Grad[8]  = {{1, 32}, {4, 5}, {6, 14}, {6, 8}, {6, 7}, {6, 5}, {6, 3}, {6, 5}};
 static const TileDefault kTileF64Mass[8]  = {{1, 32}, {1, 24}, {1, 24}, {1, 16}, {1, 8}, {1, 5}, {5, 3}, {1, 3}};
-static const TileDefault kTileF32Grad[8]  = {{5, 28}, {1, 10}, {5, 5}, {5, 3}, {5, 3}, {5, 2}, {5, 2}, {5, 2}};
-static const TileDefault kTileF32Mass[8]  = {{1, 14}, {1, 10}, {5, 10}, {5, 7}, {5, 5}, {5, 2}, {5, 2}, {5, 2}};
+static const TileDefault kTileF32Grad[8]  = {{5, 28}, {1, 10}, {5, 5}, {5, 3}, {7, 5}, {7, 2}, {7, 3}, {7, 1}};
+static const TileDefault kTileF32Mass[8]  = {{7, 32}, {1, 10}, {5, 10}, {7, 7}, {7, 5}, {7, 2}, {7, 3}, {5, 2}};
 static const TileDefault kTileF64XGrad[8] = {{1, 14}, {1, 20}, {1, 10}, {1, 7}, {6, 8}, {6, 4}, {6, 7}, {6, 5}};
 static const TileDefault kTileF64XMass[8] = {{1, 14}, {1, 16}, {1, 6}, {1, 7}, {1, 5}, {1, 6}, {5, 4}, {5, 3}};
 static const TileDefault kTileVector[8]   = {{1, 14}, {1, 8}, {1, 7}, {1, 7}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};

@@ -3,7 +3,7 @@
 For each (dim, P, Q, components, precision, QFunction, scatter) it sweeps the elements per block
 (1 up to what threads and shared memory allow), the thread-to-element mapping (Q^2-thread line slabs or
 Q^3-thread points) and, for the line mapping, the qdata staging (registers, shared memory, pipelined,
-bulk copy, or none: qdata read in the pointwise stage),
+bulk copy, persistent bulk copy one batch ahead (FP32), or none: qdata read in the pointwise stage),
 times each candidate on the device (b200_op_time: CUDA events over repeated applies on the real
 problem), keeps the fastest, and records it in a JSON cache (CEED_B200_TUNE_CACHE, default
 ~/.cache/libceed_b200/tune.json) so later operators with the same key start from the tuned tile.
@@ -17,7 +17,7 @@ import os
 from ._ffi import call
 from .ceed import F32, F64, F64X, QF_POISSON_KAPPA
 
-STAGE_NAMES = {1: "registers", 2: "shared", 3: "pipelined", 4: "point3d", 5: "bulkcopy", 6: "late"}
+STAGE_NAMES = {1: "registers", 2: "shared", 3: "pipelined", 4: "point3d", 5: "bulkcopy", 6: "late", 7: "persistent"}
 STAGE_CODES = {v: k for k, v in STAGE_NAMES.items()}
 
 
@@ -58,7 +58,7 @@ def autotune(op, u, v, reps=5, candidates=None, use_cache=True, log=None):
     qd = op._passive("qdata", u.prec)
     kap = op._passive("kappa", u.prec) if op.qf.kind == QF_POISSON_KAPPA else None
     sweep = []
-    for stage in (1, 2, 3, 4, 5, 6):
+    for stage in (1, 2, 3, 4, 5, 6, 7):
         m = ctypes.c_int()
         call("b200_op_tile_limits", fused.h, stage, ctypes.byref(m))
         epbs = candidates or sorted({e for e in (1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 14, 16, 20, 24, 28, 32) if e <= m.value})
