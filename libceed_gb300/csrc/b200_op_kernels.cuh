@@ -26,10 +26,15 @@
 //                              while batch i is computed, batch i+1's qdata streams into a second shared-memory buffer
 //                              (cp.async) and its u values and batch i+2's offsets are loaded into registers.
 //   k_op_apply<.., kStageTma>  the block's elements are consecutive, so each qdata component of the block is one
-//                              contiguous range: one thread issues one cp.async.bulk per component at entry, completing
-//                              on an mbarrier that the threads wait on (bounded) just before the pointwise stage, so the
-//                              copy overlaps the gather and the interpolation without registers or load instructions.
-//   k_op_apply<.., kStageLate> nothing staged: the pointwise stage loads each point's qdata from global memory.
+//                              contiguous range: warp 0 issues cp.async.bulk copies at entry (one per element and
+//                              component into bank-aligned slabs when elements start on 16 bytes, else one per
+//                              component), completing on an mbarrier that the threads wait on (bounded) just before the
+//                              pointwise stage, so the copy overlaps the gather and the interpolation without registers
+//                              or load instructions.  FP32: coalesced gather and scatter, per-epoch tile layouts.
+//   k_op_apply<.., kStageLate> nothing staged: the pointwise stage loads each point's qdata from global memory (after an
+//                              L2 prefetch of the block's qdata at entry).
+//   k_op_apply_ptma            FP32, one component: persistent blocks looping over element batches with the bulk-copy
+//                              staging, the next batch's copies and gathered values in flight during the current one.
 //   k_op_apply_3d              "point" mapping: a team of Q^3 threads per element, one thread per output point of
 //                              each stage (Q*P*P, Q*Q*P, Q^3, ... threads active), the 1D matrices in shared memory
 //                              and the thread's own qdata in registers (one coalesced load per component).
