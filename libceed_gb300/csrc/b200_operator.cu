@@ -197,13 +197,30 @@ static const TileDefault kTileF32Mass[8]  = {{7, 32}, {1, 10}, {5, 10}, {7, 7}, 
 static const TileDefault kTileF64XGrad[8] = {{1, 14}, {1, 20}, {1, 10}, {1, 7}, {6, 8}, {6, 4}, {6, 7}, {6, 5}};
 static const TileDefault kTileF64XMass[8] = {{1, 14}, {1, 16}, {1, 6}, {1, 7}, {1, 5}, {1, 6}, {5, 4}, {5, 3}};
 static const TileDefault kTileVector[8]   = {{1, 14}, {1, 8}, {1, 7}, {1, 7}, {1, 2}, {1, 1}, {1, 1}, {1, 1}};
+// Three-component fields at the degrees the vector sweep covers (2, 4, 6: P = 3, 5, 7), per precision and QFunction
+// ({0, 0}: fall back to kTileVector).  Indexed [P = 3, 5, 7].
+static const TileDefault kTileVecF64Grad[3]  = {{4, 4}, {4, 1}, {6, 3}};
+static const TileDefault kTileVecF64Mass[3]  = {{1, 32}, {2, 14}, {5, 5}};
+static const TileDefault kTileVecF32Grad[3]  = {{1, 10}, {5, 3}, {5, 2}};
+static const TileDefault kTileVecF32Mass[3]  = {{1, 7}, {5, 7}, {5, 2}};
+static const TileDefault kTileVecF64XGrad[3] = {{6, 32}, {6, 10}, {6, 4}};
+static const TileDefault kTileVecF64XMass[3] = {{2, 10}, {6, 8}, {6, 7}};
 
 static void op_default_tile(b200_op op, int *epb, int *stage) {
   const int   Q = op->d.Q_1d, P = op->d.P_1d;
   TileDefault t{kStageReg, 256 / (Q * Q) > 0 ? 256 / (Q * Q) : 1};
   if (P >= kOpPMin && P <= kOpPMax) {
-    const bool mass = op->d.qf == B200_QF_MASS;
-    if (op->d.num_comp > 1) t = kTileVector[P - 2];
+    const bool mass = op->d.qf == B200_QF_MASS || op->d.qf == B200_QF_VECMASS;
+    if (op->d.num_comp > 1) {
+      t = kTileVector[P - 2];
+      if (P == 3 || P == 5 || P == 7) {
+        const int         i = (P - 3) / 2;
+        const TileDefault v = op->d.prec == B200_F64    ? (mass ? kTileVecF64Mass : kTileVecF64Grad)[i]
+                              : op->d.prec == B200_F64X ? (mass ? kTileVecF64XMass : kTileVecF64XGrad)[i]
+                                                        : (mass ? kTileVecF32Mass : kTileVecF32Grad)[i];
+        t = v;
+      }
+    }
     else if (op->d.prec == B200_F64) t = (mass ? kTileF64Mass : kTileF64Grad)[P - 2];
     else if (op->d.prec == B200_F64X) t = (mass ? kTileF64XMass : kTileF64XGrad)[P - 2];
     else t = (mass ? kTileF32Mass : kTileF32Grad)[P - 2];
