@@ -350,6 +350,7 @@ def run_extras(ceed, lc, mesh, build_poisson, torch, np):
     from libceed_gb300.solver import cg_solve
 
     out = {"sweep": [], "solve": None}
+    hbm_peak = measured_peaks()[0].get("hbm_gbs", 6800.0)  # algorithmic GB/s of each family against the HBM copy rate
     ceed_det = lc.Ceed(ceed.resource, deterministic=True)
     for p in range(1, 9):
         n = N_FOR_DEGREE[p]
@@ -369,6 +370,7 @@ def run_extras(ceed, lc, mesh, build_poisson, torch, np):
             fused = objs["op"].fused(prec)
             b, f = fused.cost()
             row[tag] = {"gdofs": round(box.l_size / ms / 1e6, 4), "ms": round(ms, 4), "GBps_alg": round(b / ms / 1e6, 1),
+                        "hbm_frac": round(b / ms / 1e6 / hbm_peak, 4),
                         "tflops": round(f / ms / 1e9, 4), "tile": list(fused.tile())}
             if tag == "f64_atomic":
                 v64 = v.get_array_read()
