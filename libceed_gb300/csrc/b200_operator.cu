@@ -192,7 +192,7 @@ struct TileDefault {
 };
 static const TileDefault kTileF64Grad[8]  = {{1, 32}, {4, 5}, {6, 14}, {6, 8}, {6, 7}, {6, 5}, {6, 3}, {6, 5}};
 static const TileDefault kTileF64Mass[8]  = {{1, 32}, {1, 24}, {1, 24}, {1, 16}, {1, 8}, {1, 5}, {5, 3}, {1, 3}};
-static const TileDefault kTileF32Grad[8]  = {{5, 28}, {1, 10}, {5, 5}, {5, 3}, {7, 5}, {7, 2}, {7, 3}, {7, 1}};
+static const TileDefault kTileF32Grad[8]  = {{5, 28}, {1, 10}, {5, 5}, {7, 6}, {7, 5}, {7, 2}, {7, 3}, {7, 1}};
 static const TileDefault kTileF32Mass[8]  = {{7, 32}, {1, 10}, {5, 10}, {7, 7}, {7, 5}, {7, 2}, {7, 3}, {5, 2}};
 static const TileDefault kTileF64XGrad[8] = {{1, 14}, {1, 20}, {1, 10}, {1, 7}, {6, 8}, {6, 4}, {6, 7}, {6, 5}};
 static const TileDefault kTileF64XMass[8] = {{1, 14}, {1, 16}, {1, 6}, {1, 7}, {1, 5}, {1, 6}, {5, 4}, {5, 3}};
