@@ -759,10 +759,9 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
 // batch ahead: while batch j is computed, the values of batch j + 1 are loaded into registers (their offsets were loaded
 // one batch earlier still), and once every thread is past its last qdata read of batch j the bulk copies of batch j + 1's
 // qdata are issued into the same slabs, completing on the same mbarrier (phase parity alternating with the batch count).
-// Every copy issued is waited for, so none is in flight when a block exits.  At P = 5 the kernel is capped at 64
-// registers, which lets one more block reside per SM (measured: +3.5 % at degree 4; the cap costs at higher degrees).
+// Every copy issued is waited for, so none is in flight when a block exits.
 template <typename T, int P, int Q, int QF, bool EO>
-__global__ void __maxnreg__(P == 5 ? 64 : 255) k_op_apply_ptma(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
+__device__ __forceinline__ void op_apply_ptma(const OpArgs<typename Store<T>::type> &args, const OpMats<T, P, Q> &M) {
   static_assert(SameType<T, float>::value && QFTraits<QF>::nc == 1, "the persistent bulk-copy kernel is FP32, one component");
   using TR         = QFTraits<QF>;
   using TM         = TileMap<T, Q, kStageTma>;
@@ -895,6 +894,17 @@ __global__ void __maxnreg__(P == 5 ? 64 : 255) k_op_apply_ptma(const OpArgs<type
       u_cur[r] = u_nxt[r];
     }
   }
+}
+
+template <typename T, int P, int Q, int QF, bool EO>
+__global__ void k_op_apply_ptma(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
+  op_apply_ptma<T, P, Q, QF, EO>(args, M);
+}
+// The same kernel capped at 64 registers, used at P = 5: one more block resides per SM (measured: +3.5 % at degree 4;
+// at higher degrees the cap costs more than it gains).
+template <typename T, int P, int Q, int QF, bool EO>
+__global__ void __maxnreg__(64) k_op_apply_ptma_r64(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
+  op_apply_ptma<T, P, Q, QF, EO>(args, M);
 }
 
 // Asynchronous global -> shared copy of one 4- or 8-byte value (completes at cp.async.wait_group).

@@ -204,10 +204,17 @@ OpInstance op_instance_pipe() {
   return inst;
 }
 
+// The persistent FP32 kernel: the 64-register instance at P = 5.
+template <typename T, int P, int QF, bool EO>
+constexpr auto ptma_kernel() {
+  if constexpr (P == 5) return k_op_apply_ptma_r64<T, P, P + 1, QF, EO>;
+  else return k_op_apply_ptma<T, P, P + 1, QF, EO>;
+}
+
 template <typename T, int P, int QF, bool EO>
 int op_launch_ptma(b200_ctx ctx, const OpLaunch &r) {
   constexpr int Q    = P + 1;
-  auto          kern = k_op_apply_ptma<T, P, Q, QF, EO>;
+  auto          kern = ptma_kernel<T, P, QF, EO>();
   const size_t  smem = op_smem<T, P, QF, kStageTma>(r.epb);
   if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t nbatch = ceil_div(r.num_elem, r.epb);
@@ -220,14 +227,14 @@ int op_launch_ptma(b200_ctx ctx, const OpLaunch &r) {
 
 template <typename T, int P, int QF, bool EO>
 int op_occupancy_ptma(int epb) {
-  return blocks_per_sm(k_op_apply_ptma<T, P, P + 1, QF, EO>, epb * (P + 1) * (P + 1), op_smem<T, P, QF, kStageTma>(epb));
+  return blocks_per_sm(ptma_kernel<T, P, QF, EO>(), epb * (P + 1) * (P + 1), op_smem<T, P, QF, kStageTma>(epb));
 }
 
 template <typename T, int P, int QF, bool EO>
 OpInstance op_instance_ptma() {
   OpInstance         inst{op_launch_ptma<T, P, QF, EO>, op_smem<T, P, QF, kStageTma>, op_occupancy_ptma<T, P, QF, EO>, 1024, true};
   cudaFuncAttributes attr;
-  if (cudaFuncGetAttributes(&attr, k_op_apply_ptma<T, P, P + 1, QF, EO>) == cudaSuccess) inst.max_threads = attr.maxThreadsPerBlock;
+  if (cudaFuncGetAttributes(&attr, ptma_kernel<T, P, QF, EO>()) == cudaSuccess) inst.max_threads = attr.maxThreadsPerBlock;
   return inst;
 }
 
