@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_pdot(int64_t n, const T *
   constexpr int U      = kUnroll<T>;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double        acc    = 0.0;
+  typename AccFor<T>::type acc;
   for (; i + (U - 1) * stride < n; i += U * stride) {
     T wv[U], pv[U];
 #pragma unroll
@@ -40,11 +40,11 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_pdot(int64_t n, const T *
       pv[k] = p[i + k * stride];
     }
 #pragma unroll
-    for (int k = 0; k < U; k++) acc += (double)pv[k] * (double)wv[k];
+    for (int k = 0; k < U; k++) acc.add_prod(pv[k], wv[k]);
   }
-  for (; i < n; i += stride) acc += (double)p[i] * (double)w[i];
-  acc = block_reduce(kRedDot, acc);
-  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+  for (; i < n; i += stride) acc.add_prod(p[i], w[i]);
+  const double sum = block_reduce(kRedDot, acc.value());
+  if (threadIdx.x == 0) partial[blockIdx.x] = sum;
 }
 
 // x += alpha p, r = m (r - alpha w), and the partial sums of r.r.  The mask (0 or 1) applied here is the m of m A(m x):
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const d
   const T       alpha  = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double        acc    = 0.0;
+  typename AccFor<T>::type acc;
   for (; i + (U - 1) * stride < n; i += U * stride) {
     T xv[U], pv[U], rv[U], wv[U], mv[U];
 #pragma unroll
@@ -74,17 +74,17 @@ __global__ void __launch_bounds__(kReduceThreads) k_cg_update(int64_t n, const d
       x[i + k * stride] = xv[k] + alpha * pv[k];
       const T ri        = mv[k] * (rv[k] - alpha * wv[k]);
       r[i + k * stride] = ri;
-      acc += (double)ri * (double)ri;
+      acc.add_prod(ri, ri);
     }
   }
   for (; i < n; i += stride) {
     x[i] += alpha * p[i];
     const T ri = mask[i] * (r[i] - alpha * w[i]);
     r[i]       = ri;
-    acc += (double)ri * (double)ri;
+    acc.add_prod(ri, ri);
   }
-  acc = block_reduce(kRedSumSq, acc);
-  if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+  const double sum = block_reduce(kRedSumSq, acc.value());
+  if (threadIdx.x == 0) partial[blockIdx.x] = sum;
 }
 
 // Preconditioned update: also z = M r, with partial sums of r.z (partial) and r.r (partial2).
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const 
   const T       alpha  = (T)(pw != 0.0 ? s[kRR] / pw : 0.0);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double        rz = 0.0, rr = 0.0;
+  typename AccFor<T>::type rz, rr;
   for (; i + (U - 1) * stride < n; i += U * stride) {
     T xv[U], pv[U], rv[U], wv[U], dv[U], mv[U];
 #pragma unroll
@@ -117,8 +117,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const 
       const T zi        = dv[k] * ri;
       r[i + k * stride] = ri;
       z[i + k * stride] = zi;
-      rz += (double)ri * (double)zi;
-      rr += (double)ri * (double)ri;
+      rz.add_prod(ri, zi);
+      rr.add_prod(ri, ri);
     }
   }
   for (; i < n; i += stride) {
@@ -127,15 +127,15 @@ __global__ void __launch_bounds__(kReduceThreads) k_pcg_update(int64_t n, const 
     const T zi = inv_diag[i] * ri;
     r[i]       = ri;
     z[i]       = zi;
-    rz += (double)ri * (double)zi;
-    rr += (double)ri * (double)ri;
+    rz.add_prod(ri, zi);
+    rr.add_prod(ri, ri);
   }
-  rz = block_reduce(kRedDot, rz);
+  const double rz_sum = block_reduce(kRedDot, rz.value());
   __syncthreads();
-  rr = block_reduce(kRedSumSq, rr);
+  const double rr_sum = block_reduce(kRedSumSq, rr.value());
   if (threadIdx.x == 0) {
-    partial[blockIdx.x]  = rz;
-    partial2[blockIdx.x] = rr;
+    partial[blockIdx.x]  = rz_sum;
+    partial2[blockIdx.x] = rr_sum;
   }
 }
 

@@ -17,6 +17,40 @@ inline int reduce_blocks(int num_sms) { return 2 * num_sms; }
 
 __device__ __forceinline__ double red_combine(int kind, double a, double b) { return kind == kRedMaxAbs ? fmax(a, b) : a + b; }
 
+// Per-thread accumulators.  FP64 data: a double.  FP32 data: a float-float sum (~48 bits) on the FP32 pipe -- each
+// product's rounding error from an FMA (the product itself by __fmul_rn, so that it is not contracted into the sum)
+// and each addition's from Knuth's TwoSum, collected in the low word -- instead of converting every value to double,
+// which on this GPU puts two conversions and a multiply-add per element on the FP64 pipe (1/60 of the FP32 rate) and
+// bounded the FP32 CG's dot products at a fifth of the HBM rate.
+struct DAcc {
+  double                            s = 0.0;
+  __device__ __forceinline__ void   add(double v) { s += v; }
+  __device__ __forceinline__ void   add_prod(double a, double b) { s += a * b; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+struct F2Acc {
+  float                           hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float s = __fadd_rn(hi, v), bb = __fsub_rn(s, hi);
+    lo            = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+    hi            = s;
+  }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    lo            = __fadd_rn(lo, __fmaf_rn(a, b, -p));
+    add(p);
+  }
+  __device__ __forceinline__ double value() const { return isfinite(hi) ? (double)hi + (double)lo : (double)hi; }
+};
+template <typename T>
+struct AccFor {
+  using type = DAcc;
+};
+template <>
+struct AccFor<float> {
+  using type = F2Acc;
+};
+
 // Block-wide combine in a fixed tree: warp shuffles, then the warp leaders.
 __device__ __forceinline__ double block_reduce(int kind, double v) {
   __shared__ double s_warp[kReduceThreads / 32];
@@ -30,15 +64,6 @@ __device__ __forceinline__ double block_reduce(int kind, double v) {
   return v;
 }
 
-__device__ __forceinline__ double red_term(int kind, double acc, double xi, double yi) {
-  switch (kind) {
-    case kRedSumSq: return acc + xi * xi;
-    case kRedAbsSum: return acc + fabs(xi);
-    case kRedMaxAbs: return fmax(acc, fabs(xi));
-    default: return acc + xi * yi;
-  }
-}
-
 // The fixed grid leaves few threads per SM, so each thread loads 8 elements (i, i + stride, ...) before combining
 // them; the combination order is the plain loop's, so the result does not depend on the unrolling.
 template <typename T>
@@ -47,7 +72,17 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_partial(int kind, int
   constexpr int U      = 8;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t       i      = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  double        acc    = 0.0;
+  // The vector API's norms and dots keep FP64 sums for FP32 data too, so that squares above the FP32 range (|x| > 1.8e19)
+  // do not overflow; the CG kernels, whose vectors are scaled to unit norm, use the FP32-pipe accumulator.
+  DAcc sum;           // kRedSumSq, kRedAbsSum, kRedDot
+  T    mx = T(0);     // kRedMaxAbs
+  auto term = [&](T xi, T yi) {
+    const T ax = xi < T(0) ? -xi : xi;
+    if (kind == kRedSumSq) sum.add_prod((double)xi, (double)xi);
+    else if (kind == kRedAbsSum) sum.add((double)ax);
+    else if (kind == kRedMaxAbs) mx = ax > mx ? ax : mx;
+    else sum.add_prod((double)xi, (double)yi);
+  };
   for (; i + (U - 1) * stride < n; i += U * stride) {
     T xv[U], yv[U];
 #pragma unroll
@@ -56,10 +91,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_partial(int kind, int
       yv[k] = kind == kRedDot ? y[i + k * stride] : T(0);
     }
 #pragma unroll
-    for (int k = 0; k < U; k++) acc = red_term(kind, acc, (double)xv[k], (double)yv[k]);
+    for (int k = 0; k < U; k++) term(xv[k], yv[k]);
   }
-  for (; i < n; i += stride) acc = red_term(kind, acc, (double)x[i], kind == kRedDot ? (double)y[i] : 0.0);
-  acc = block_reduce(kind, acc);
+  for (; i < n; i += stride) term(x[i], kind == kRedDot ? y[i] : T(0));
+  const double acc = block_reduce(kind, kind == kRedMaxAbs ? (double)mx : sum.value());
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
