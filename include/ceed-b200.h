@@ -173,6 +173,15 @@ int b200_op_create(b200_ctx ctx, const b200_op_desc *desc, b200_op *op);
  * the operator's storage precision (double for B200_F64 and B200_F64X); kappa: [elem][qpt] or NULL.  With no elements
  * Apply zeroes v and ApplyAdd leaves it; u and qdata may then be NULL. */
 int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add);
+/* v = A u together with u . (A u), for CG-type solvers (no counterpart in the reference, whose solvers take the dot
+ * product in a separate pass).  Only for operators whose kernel is the persistent FP32 one (staging 7) with the atomic
+ * scatter: b200_op_dot_len sets *blocks to the number of per-block partial sums (0: not available for this operator, and
+ * b200_op_apply_dot returns B200_ERROR_UNSUPPORTED) and *doubles to the length of the device array `partial` that
+ * b200_op_apply_dot needs (at least *blocks).  After the apply, partial[0 .. *blocks) hold the per-block sums (FP64; the
+ * kernel sums each thread's quadrature-point terms (grad u)^T D (grad u), or u q u for the mass, in float-float).
+ * Their sum, in order, is u . (A u) (exact for the assembled operator: u . A u = sum over elements of u_e . A_e u_e). */
+int b200_op_dot_len(b200_op op, int *blocks, int64_t *doubles);
+int b200_op_apply_dot(b200_op op, const void *u, void *v, const void *qdata, double *partial);
 /* Algorithmic bytes and FLOPs of one apply (for roofline reporting). */
 int b200_op_cost(b200_op op, double *bytes, double *flops);
 /* The reference's FLOP model of one apply of a fused operator, CeedOperatorGetFlopsEstimate
@@ -234,7 +243,8 @@ int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qda
 /* ---- Conjugate gradients on the fused operator (no libCEED counterpart: the reference solves with PETSc KSPCG around
  *      CeedOperatorApply in examples/petsc/bps.c).  Homogeneous Dirichlet conditions through mask (exactly 1 free, 0 fixed):
  *      solves m A(m x) = m b from x = 0.  mixed = 0: FP64 CG.  mixed = 1: FP32 CG (op32, qdata32) on the defect
- *      r = m(b - A64 x), computed in FP64, until |r| / |b| <= rtol.  Dot products and norms accumulate in FP64.
+ *      r = m(b - A64 x), computed in FP64, until |r| / |b| <= rtol.  Dot products and norms are summed per thread in FP64
+ *      (FP64 vectors) or float-float (FP32 vectors), then in FP64, in a fixed order.
  *      Blocks of check_every iterations run as one CUDA graph when use_graph = 1.  b, x, mask: FP64 device arrays
  *      of length n.  With jacobi set (e.g. from b200_assemble_diagonal), the iterations are Jacobi-preconditioned. */
 typedef struct {
@@ -246,6 +256,8 @@ typedef struct {
   int    use_graph;   /* capture iteration blocks in CUDA graphs */
   int    check_every; /* iterations between convergence checks (graph size) */
   const double *jacobi; /* Jacobi preconditioner: masked 1/diag(A) (FP64, device, length n), or NULL for plain CG */
+  int    separate_pdot; /* mixed: 1 takes p.(A p) in a pass over p and A p even where the FP32 operator's persistent kernel
+                           sums it element by element during the apply (0, the default) */
 } b200_cg_opts;
 
 typedef struct {

@@ -37,6 +37,7 @@ class CGOpts(ctypes.Structure):
     _fields_ = [
         ("rtol", ctypes.c_double), ("max_it", ctypes.c_int), ("mixed", ctypes.c_int), ("inner_rtol", ctypes.c_double),
         ("max_outer", ctypes.c_int), ("use_graph", ctypes.c_int), ("check_every", ctypes.c_int), ("jacobi", ctypes.c_void_p),
+        ("separate_pdot", ctypes.c_int),
     ]
 
 

@@ -572,6 +572,22 @@ class Operator:
         """CeedOperatorApplyAdd: v += A u."""
         self._apply(u, v, True)
 
+    def apply_dot(self, u, v):
+        """v = A u, returning u . (A u) as the persistent FP32 kernel (staging 7, atomic scatter) sums it during the
+        apply (b200_op_apply_dot); raises B200Error for operators whose kernel has no such form."""
+        op = self._fused_op(self._kernel_prec(u.prec))
+        qd = self._passive("qdata", u.prec)
+        nb, n = ctypes.c_int(), ctypes.c_int64()
+        call("b200_op_dot_len", op.h, ctypes.byref(nb), ctypes.byref(n))
+        if nb.value == 0:
+            raise B200Error("b200_op_apply_dot", -2, "u . (A u) during the apply needs the persistent FP32 kernel (staging 7)")
+        part = torch.empty(n.value, dtype=torch.float64, device=self.ceed.device)
+        call("b200_op_apply_dot", op.h, u.ptr(), v.ptr(), qd.ptr(), _vp(part.data_ptr()))
+        total = 0.0
+        for x in part[: nb.value].cpu().tolist():  # in block order, as the CG's final pass adds them
+            total += x
+        return total
+
     def get_flops_estimate(self):
         """CeedOperatorGetFlopsEstimate: the reference's FLOP model of one apply (b200_flops_estimate)."""
         f = self._active_input()

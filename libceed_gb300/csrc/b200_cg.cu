@@ -5,8 +5,9 @@
 // mask (1 on free nodes, 0 on the box boundary): the solver works with m * A(m * x).
 //
 // All scalars (alpha, beta, r.r) stay on the device, so a block of `check_every` iterations is one CUDA graph and the
-// host only reads r.r between blocks.  Dot products and norms are accumulated in FP64 with the fixed-order two-pass
-// reduction, also for FP32 vectors.  Mixed mode (defect correction): r = m(b - A64 x) in FP64; FP32 CG solves
+// host only reads r.r between blocks.  Dot products and norms use a fixed-order two-pass reduction: each thread sums
+// in FP64 for FP64 vectors and in float-float (about 48 bits, on the FP32 pipe) for FP32 vectors, and the per-block
+// and final passes add in FP64.  Mixed mode (defect correction): r = m(b - A64 x) in FP64; FP32 CG solves
 // A32 d = r to a relative tolerance; x += d in FP64; repeat until |r| / |b| <= rtol.
 #include "b200_internal.cuh"
 #include "b200_reduce.cuh"
@@ -243,6 +244,8 @@ struct CgWork {
   int64_t  n;
   int      blocks;
   double  *partial, *partial2, *s, *s_host;
+  double  *dot_partial;  // per-block p.w of the fused apply (persistent FP32 operator), dot_blocks of them, then its scratch
+  int      dot_blocks;
   double  *r64, *p64, *w64, *z64;
   float   *x32, *r32, *p32, *w32, *z32, *mask32, *inv32;
   const double *inv64;  // Jacobi preconditioner (masked 1/diag) or nullptr
@@ -252,13 +255,22 @@ template <typename T>
 static int cg_iterations(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *x, T *r, T *p, T *w, T *z, const T *inv, int count) {
   b200_ctx  ctx = wk.ctx;
   const int g   = wk.blocks;
+  // The persistent FP32 operator sums p.w = p.(A p) element by element inside the apply, which saves the pass over p and w.
+  const int db = wk.dot_partial ? op_dot_blocks(op, nullptr) : 0;
   for (int it = 0; it < count; it++) {
-    int st = b200_op_apply(op, p, w, qdata, nullptr, 0);
-    if (st) return st;
-    k_cg_pdot<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, p, w, wk.partial);
-    B200_LAUNCHED(ctx, "cg_pdot");
-    k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kPW, 1);
-    B200_LAUNCHED(ctx, "cg_final");
+    if (db > 0) {
+      int st = op_apply_dot(op, p, w, qdata, wk.dot_partial);
+      if (st) return st;
+      k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(db, wk.dot_partial, wk.s, kPW, 1);
+      B200_LAUNCHED(ctx, "cg_final");
+    } else {
+      int st = b200_op_apply(op, p, w, qdata, nullptr, 0);
+      if (st) return st;
+      k_cg_pdot<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, p, w, wk.partial);
+      B200_LAUNCHED(ctx, "cg_pdot");
+      k_cg_final<<<1, kReduceThreads, 0, ctx->stream>>>(g, wk.partial, wk.s, kPW, 1);
+      B200_LAUNCHED(ctx, "cg_final");
+    }
     if (inv) {
       k_pcg_update<T><<<g, kReduceThreads, 0, ctx->stream>>>(wk.n, wk.s, mask, x, r, z, inv, p, w, wk.partial, wk.partial2);
       B200_LAUNCHED(ctx, "pcg_update");
@@ -410,6 +422,9 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
   B200_CUDA(cudaMalloc(&wk.p64, sizeof(double) * (size_t)n));
   B200_CUDA(cudaMalloc(&wk.w64, sizeof(double) * (size_t)n));
   if (opts->mixed) {
+    size_t dot_len = 0;
+    wk.dot_blocks  = opts->separate_pdot ? 0 : op_dot_blocks(op32, &dot_len);
+    if (wk.dot_blocks > 0) B200_CUDA(cudaMalloc(&wk.dot_partial, sizeof(double) * dot_len));
     B200_CUDA(cudaMalloc(&wk.x32, sizeof(float) * (size_t)n));
     B200_CUDA(cudaMalloc(&wk.r32, sizeof(float) * (size_t)n));
     B200_CUDA(cudaMalloc(&wk.p32, sizeof(float) * (size_t)n));
@@ -492,6 +507,7 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
   cudaEventDestroy(e1);
   cudaFree(wk.partial);
   cudaFree(wk.partial2);
+  cudaFree(wk.dot_partial);
   cudaFree(wk.z64);
   cudaFree(wk.z32);
   cudaFree(wk.inv32);

@@ -156,6 +156,24 @@ __device__ __forceinline__ dfloat operator-(const dfloat &a) {
   return r;
 }
 __device__ __forceinline__ dfloat operator-(const dfloat &a, const dfloat &b) { return a + (-b); }
+
+// Running sum of FP32 terms in float-float (about 48 bits): each addition's rounding error from Knuth's TwoSum and
+// each product's from an FMA (the product itself by __fmul_rn, so that it is not contracted into the sum) are
+// collected in the low word.  Used by sums and dot products over FP32 vectors.
+struct F2Acc {
+  float                           hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float s = __fadd_rn(hi, v), bb = __fsub_rn(s, hi);
+    lo            = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+    hi            = s;
+  }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    lo            = __fadd_rn(lo, __fmaf_rn(a, b, -p));
+    add(p);
+  }
+  __device__ __forceinline__ double value() const { return isfinite(hi) ? (double)hi + (double)lo : (double)hi; }
+};
 __device__ __forceinline__ dfloat &operator+=(dfloat &a, const dfloat &b) { return a = a + b; }
 __device__ __forceinline__ dfloat &operator*=(dfloat &a, const dfloat &b) { return a = a * b; }
 

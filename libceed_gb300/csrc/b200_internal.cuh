@@ -42,6 +42,12 @@ inline int stride_grid(b200_ctx ctx, int64_t n, int threads) {
   return (int)(want < cap ? want : cap);
 }
 
+// Fused w = A u and u . (A u) for the CG (persistent FP32 operators with the atomic scatter): op_dot_blocks returns
+// how many per-block partial sums op_apply_dot writes at the start of `partial`, or 0 when the operator's kernel has no
+// such form, and sets *doubles to the length `partial` needs (the partial sums, then the kernel's per-thread scratch).
+int op_dot_blocks(b200_op op, size_t *doubles);
+int op_apply_dot(b200_op op, const void *u, void *v, const void *qdata, double *partial);
+
 }  // namespace b200
 
 #define B200_CUDA(call)                                                                  \

@@ -227,6 +227,7 @@ struct OpArgs {
   const T       *qdata;  // [qcomp][elem][qpt]
   const T       *kappa;  // [elem][qpt] or nullptr
   int           *status; // device status word (B200_STATUS_* bits)
+  double        *dot;    // persistent FP32 kernel: per-block sums of u . (A u) over its elements, or nullptr
 };
 
 template <int QF>
@@ -307,6 +308,11 @@ __host__ __device__ constexpr size_t tma_prefix_bytes(int epb) {
 
 struct NoWait {
   __device__ void operator()() const {}
+};
+// Per-point hook of op_stages: receives each quadrature point's term of u . (A u) (grad u . D grad u, or u q u).
+struct NoDot {
+  __device__ void operator()(float) const {}
+  __device__ void operator()(double) const {}
 };
 
 // out[j] = sum_k M[j*K + k] in[k], j < J
@@ -407,10 +413,12 @@ struct Contract {
 // thread has passed a barrier after writing them; qd(k, z) returns qdata component k (kappa already applied) at point
 // (a, b, z), after qwait() has returned; qafter() runs once all threads are past their last qdata read.  On exit the
 // x-line owners hold in out[p] the element result at node (p, lx.u, lx.w) of team lx.team.  Uses the three tile buffers
-// of `tl` (each epoch in its own layout) and block-wide barriers.
-template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename TL, typename QD, typename QW = NoWait, typename QA = NoWait>
+// of `tl` (each epoch in its own layout) and block-wide barriers.  qdot(t) receives each of the thread's quadrature
+// points' terms of u . (A u) = sum over points of (grad u)^T D (grad u) (mass: u q u).
+template <typename T, int P, int Q, int QF, bool EO, bool XREG, typename TL, typename QD, typename QW = NoWait, typename QA = NoWait,
+          typename QP = NoDot>
 __device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M, int a, int b, const LineOwner &lx, const LineOwner &ly,
-                                          const T (&xin)[P], QD qd, T (&out)[P], QW qwait = QW{}, QA qafter = QA{}) {
+                                          const T (&xin)[P], QD qd, T (&out)[P], QW qwait = QW{}, QA qafter = QA{}, QP qdot = QP{}) {
   using C             = Contract<T, P, Q, EO>;
   constexpr bool GRAD = QFTraits<QF>::grad;
   // ---- X interpolation: lines (y, z) < P, owner lx ------------------------------------------------------------------
@@ -469,8 +477,10 @@ __device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M
       T D[6];
 #pragma unroll
       for (int k = 0; k < 6; k++) D[k] = qd(k, z);
-      T vg[3];
-      poisson_point(D, tl.template at<kEpDX>(0, a, b, z), tl.template at<kEpDY>(2, a, b, z), dz[z], vg);
+      T       vg[3];
+      const T gx = tl.template at<kEpDX>(0, a, b, z), gy = tl.template at<kEpDY>(2, a, b, z);
+      poisson_point(D, gx, gy, dz[z], vg);
+      if constexpr (!SameType<QP, NoDot>::value) qdot(gx * vg[0] + gy * vg[1] + dz[z] * vg[2]);
       tl.template at<kEpDX>(0, a, b, z) = vg[0];
       tl.template at<kEpDY>(2, a, b, z) = vg[1];
       dz[z]                 = vg[2];
@@ -513,7 +523,10 @@ __device__ __forceinline__ void op_stages(const TL &tl, const OpMats<T, P, Q> &M
     T w[Q], o[P];
     qwait();
 #pragma unroll
-    for (int z = 0; z < Q; z++) w[z] = U[z] * qd(0, z);
+    for (int z = 0; z < Q; z++) {
+      w[z] = U[z] * qd(0, z);
+      if constexpr (!SameType<QP, NoDot>::value) qdot(U[z] * w[z]);
+    }
     C::interp_t(M, w, o);
     if constexpr (!TL::same(kEpYZ, kEpZT)) __syncthreads();
 #pragma unroll
@@ -760,7 +773,11 @@ __global__ void k_op_apply(const OpArgs<typename Store<T>::type> args, const OpM
 // one batch earlier still), and once every thread is past its last qdata read of batch j the bulk copies of batch j + 1's
 // qdata are issued into the same slabs, completing on the same mbarrier (phase parity alternating with the batch count).
 // Every copy issued is waited for, so none is in flight when a block exits.
-template <typename T, int P, int Q, int QF, bool EO>
+// DOT: also write to args.dot[blockIdx.x] the block's share of u . (A u), summed per thread in float-float over the
+// quadrature points of its active elements (in two floats per thread after the tile buffers) and then per block in
+// FP64, in a fixed order (a CG step's p . A p without a
+// second pass over the vectors; exact for the assembled operator, since u . (A u) = sum over elements of u_e . (A_e u_e)).
+template <typename T, int P, int Q, int QF, bool EO, bool DOT>
 __device__ __forceinline__ void op_apply_ptma(const OpArgs<typename Store<T>::type> &args, const OpMats<T, P, Q> &M) {
   static_assert(SameType<T, float>::value && QFTraits<QF>::nc == 1, "the persistent bulk-copy kernel is FP32, one component");
   using TR         = QFTraits<QF>;
@@ -827,7 +844,13 @@ __device__ __forceinline__ void op_apply_ptma(const OpArgs<typename Store<T>::ty
   };
 
   int64_t batch = blockIdx.x;
-  if (batch >= nbatch) return;
+  if (batch >= nbatch) {
+    if (DOT && threadIdx.x == 0) args.dot[blockIdx.x] = 0.0;
+    return;
+  }
+  // DOT: the running sums (registers held across the loop spill at 64 per thread); each thread only touches its own.
+  auto dot_slot = [&]() -> float * { return reinterpret_cast<float *>(tiles + 3 * TM::region(args.epb)) + 2 * threadIdx.x; };
+  if (DOT) dot_slot()[0] = dot_slot()[1] = 0.f;
   if (threadIdx.x == 0) mbar_init(bar, 1);
   __syncthreads();
   issue(batch);
@@ -869,7 +892,13 @@ __device__ __forceinline__ void op_apply_ptma(const OpArgs<typename Store<T>::ty
       else return T(sl[k * st + qoff[k] + q]);
     };
     T none[P], out[P];
-    op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, lx, ly, none, qd, out, qwait, qafter);
+    T pts = T(0);  // DOT: this batch's points
+    if constexpr (DOT) {
+      auto qdot = [&](T t) { pts += t; };
+      op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, lx, ly, none, qd, out, qwait, qafter, qdot);
+    } else {
+      op_stages<T, P, Q, QF, EO, false>(tl, M, a, b, lx, ly, none, qd, out, qwait, qafter);
+    }
     // Buffer 0 was last read by the Y interpolation (transposed), before the barrier that preceded the X stage.
     if (lx.on) {
 #pragma unroll
@@ -893,18 +922,46 @@ __device__ __forceinline__ void op_apply_ptma(const OpArgs<typename Store<T>::ty
       o_nxt[r] = o_nn[r];
       u_cur[r] = u_nxt[r];
     }
+    if (DOT && active) {  // inactive teams hold stale qdata: their sum is dropped
+      float *sl = dot_slot();
+      F2Acc  acc;
+      acc.hi = sl[0], acc.lo = sl[1];
+      acc.add(pts);
+      sl[0] = acc.hi, sl[1] = acc.lo;
+    }
+  }
+  if constexpr (DOT) {
+    // Block sum through the (now free) tile buffers: thread t < 32 adds entries t, t + 32, ... (only thread t touches
+    // entry t), then thread 0 adds those 32.
+    double *red = reinterpret_cast<double *>(tiles);
+    F2Acc   acc;
+    acc.hi = dot_slot()[0], acc.lo = dot_slot()[1];
+    __syncthreads();
+    red[threadIdx.x] = acc.value();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double t = 0.0;
+      for (int i = threadIdx.x; i < (int)blockDim.x; i += 32) t += red[i];
+      red[threadIdx.x] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int i = 0; i < 32 && i < (int)blockDim.x; i++) t += red[i];
+      args.dot[blockIdx.x] = t;
+    }
   }
 }
 
-template <typename T, int P, int Q, int QF, bool EO>
+template <typename T, int P, int Q, int QF, bool EO, bool DOT>
 __global__ void k_op_apply_ptma(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
-  op_apply_ptma<T, P, Q, QF, EO>(args, M);
+  op_apply_ptma<T, P, Q, QF, EO, DOT>(args, M);
 }
 // The same kernel capped at 64 registers, used at P = 5: one more block resides per SM (measured: +3.5 % at degree 4;
 // at higher degrees the cap costs more than it gains).
-template <typename T, int P, int Q, int QF, bool EO>
+template <typename T, int P, int Q, int QF, bool EO, bool DOT>
 __global__ void __maxnreg__(64) k_op_apply_ptma_r64(const OpArgs<typename Store<T>::type> args, const OpMats<T, P, Q> M) {
-  op_apply_ptma<T, P, Q, QF, EO>(args, M);
+  op_apply_ptma<T, P, Q, QF, EO, DOT>(args, M);
 }
 
 // Asynchronous global -> shared copy of one 4- or 8-byte value (completes at cp.async.wait_group).

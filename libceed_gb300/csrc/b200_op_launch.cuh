@@ -26,6 +26,7 @@ struct OpLaunch {
   void          *v, *e_out, *g;
   const double  *B, *G;  // host 1D matrices, Q x P and Q x Q
   int           *status;  // device status word of the context
+  double        *dot;     // persistent FP32 kernel: per-block sums of u . (A u) (one per block of the grid), or nullptr
 };
 
 using OpLauncher  = int (*)(b200_ctx ctx, const OpLaunch &req);
@@ -38,6 +39,7 @@ struct OpInstance {
   OpOccupancy occupancy;
   int         max_threads;  // from cudaFuncGetAttributes (register-limited)
   bool        persistent;
+  OpOccupancy dot_occupancy = nullptr;  // persistent FP32 kernel: blocks per SM of its form that also sums u . (A u)
 };
 
 // Even-odd form of a row-major J x K matrix M with parity par (+1 or -1).
@@ -90,6 +92,7 @@ inline OpArgs<typename Store<T>::type> make_args(const OpLaunch &r) {
   a.qdata       = (const S *)r.qdata;
   a.kappa       = (const S *)r.kappa;
   a.status      = r.status;
+  a.dot         = r.dot;
   return a;
 }
 
@@ -205,34 +208,43 @@ OpInstance op_instance_pipe() {
 }
 
 // The persistent FP32 kernel: the 64-register instance at P = 5.
-template <typename T, int P, int QF, bool EO>
+template <typename T, int P, int QF, bool EO, bool DOT = false>
 constexpr auto ptma_kernel() {
-  if constexpr (P == 5) return k_op_apply_ptma_r64<T, P, P + 1, QF, EO>;
-  else return k_op_apply_ptma<T, P, P + 1, QF, EO>;
+  if constexpr (P == 5) return k_op_apply_ptma_r64<T, P, P + 1, QF, EO, DOT>;
+  else return k_op_apply_ptma<T, P, P + 1, QF, EO, DOT>;
 }
 
+// The DOT form keeps each thread's running float-float sum (two floats) after the tile buffers.
+template <typename T, int P, int QF, bool DOT>
+size_t op_smem_ptma(int epb) {
+  return op_smem<T, P, QF, kStageTma>(epb) + (DOT ? (size_t)epb * (P + 1) * (P + 1) * 2 * sizeof(float) : 0);
+}
+
+// With r.dot set, the DOT instance also writes one partial sum of u . (A u) per block, r.grid of them (blocks past
+// the last batch write 0).
 template <typename T, int P, int QF, bool EO>
 int op_launch_ptma(b200_ctx ctx, const OpLaunch &r) {
   constexpr int Q    = P + 1;
-  auto          kern = ptma_kernel<T, P, QF, EO>();
-  const size_t  smem = op_smem<T, P, QF, kStageTma>(r.epb);
+  auto          kern = r.dot ? ptma_kernel<T, P, QF, EO, true>() : ptma_kernel<T, P, QF, EO>();
+  const size_t  smem = r.dot ? op_smem_ptma<T, P, QF, true>(r.epb) : op_smem_ptma<T, P, QF, false>(r.epb);
   if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t nbatch = ceil_div(r.num_elem, r.epb);
-  const int64_t grid   = r.grid < nbatch ? r.grid : nbatch;
+  const int64_t grid   = r.dot ? r.grid : (r.grid < nbatch ? r.grid : nbatch);
   if (grid <= 0) return B200_SUCCESS;
   kern<<<(unsigned)grid, r.epb * Q * Q, smem, ctx->stream>>>(make_args<T>(r), make_mats<T, P, Q>(r.B, r.G));
   B200_LAUNCHED(ctx, "op_apply_ptma");
   return B200_SUCCESS;
 }
 
-template <typename T, int P, int QF, bool EO>
+template <typename T, int P, int QF, bool EO, bool DOT>
 int op_occupancy_ptma(int epb) {
-  return blocks_per_sm(ptma_kernel<T, P, QF, EO>(), epb * (P + 1) * (P + 1), op_smem<T, P, QF, kStageTma>(epb));
+  return blocks_per_sm(ptma_kernel<T, P, QF, EO, DOT>(), epb * (P + 1) * (P + 1), op_smem_ptma<T, P, QF, DOT>(epb));
 }
 
 template <typename T, int P, int QF, bool EO>
 OpInstance op_instance_ptma() {
-  OpInstance         inst{op_launch_ptma<T, P, QF, EO>, op_smem<T, P, QF, kStageTma>, op_occupancy_ptma<T, P, QF, EO>, 1024, true};
+  OpInstance inst{op_launch_ptma<T, P, QF, EO>, op_smem<T, P, QF, kStageTma>, op_occupancy_ptma<T, P, QF, EO, false>, 1024, true,
+                  op_occupancy_ptma<T, P, QF, EO, true>};
   cudaFuncAttributes attr;
   if (cudaFuncGetAttributes(&attr, ptma_kernel<T, P, QF, EO>()) == cudaSuccess) inst.max_threads = attr.maxThreadsPerBlock;
   return inst;

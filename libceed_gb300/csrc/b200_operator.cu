@@ -150,6 +150,7 @@ struct b200_op_s {
   OpInstance          inst;
   int                 stage, epb, variant;
   int                 grid;       // persistent variant: blocks
+  int                 dot_grid;   // persistent FP32 kernel: blocks of its form that also sums u . (A u), else 0
   bool                symmetric;  // B centro-symmetric and G_c centro-antisymmetric: even-odd kernels apply
   b200_plan           plan;     // deterministic scatter only
   void               *e_work;   // element results for the deterministic scatter, [comp][elem][node]
@@ -254,17 +255,19 @@ static int op_select(b200_op op, int epb, int stage) {
   if (epb > max_epb_threads) epb = max_epb_threads;
   if (epb > max_epb_smem) epb = max_epb_smem;
   B200_CHECK(epb >= 1 && inst.smem(epb) <= 227 * 1024, B200_ERROR_UNSUPPORTED, "fused kernel P=%d does not fit one element per block", op->d.P_1d);
-  int grid = 0;
+  int grid = 0, dot_grid = 0;
   if (inst.persistent) {
     const int occ = inst.occupancy(epb);
     B200_CHECK(occ >= 1, B200_ERROR_UNSUPPORTED, "pipelined kernel P=%d with %d elements per block cannot be resident", op->d.P_1d, epb);
     grid = occ * op->ctx->num_sms;
+    if (inst.dot_occupancy) dot_grid = inst.dot_occupancy(epb) * op->ctx->num_sms;
   }
   op->inst    = inst;
   op->stage   = stage;
   op->epb     = epb;
   op->variant = variant;
   op->grid    = grid;
+  op->dot_grid = dot_grid;
   return B200_SUCCESS;
 }
 
@@ -321,7 +324,7 @@ extern "C" int b200_op_get_tile(b200_op op, int *elems_per_block, int *threads_p
   return B200_SUCCESS;
 }
 
-extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add) {
+static int op_apply_impl(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add, double *dot) {
   b200_ctx            ctx = op->ctx;
   const b200_op_desc &d   = op->d;
   B200_CHECK(!op->jit, B200_ERROR_INCOMPATIBLE, "operator has a run-time compiled QFunction: use b200_op_apply_jit");
@@ -337,7 +340,7 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   r.num_elem    = d.num_elem;
   r.comp_stride = d.comp_stride;
   r.epb         = op->epb;
-  r.grid        = op->grid;
+  r.grid        = dot ? op->dot_grid : op->grid;
   r.det         = d.scatter == B200_SCATTER_DETERMINISTIC;
   r.offsets     = d.offsets;
   r.u           = u;
@@ -348,11 +351,42 @@ extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qda
   r.B           = op->B.data();
   r.G           = op->Gc.data();
   r.status      = ctx->d_status;
+  r.dot         = dot;
   if (!r.det && !add) B200_CUDA(cudaMemsetAsync(v, 0, tsz * (size_t)d.l_size, ctx->stream));
   int st = op->inst.launch(ctx, r);
   if (st) return st;
   if (r.det) st = plan_scatter(op->plan, storage_prec(d.prec), op->e_work, v, add);
   return st;
+}
+
+extern "C" int b200_op_apply(b200_op op, const void *u, void *v, const void *qdata, const void *kappa, int add) {
+  return op_apply_impl(op, u, v, qdata, kappa, add, nullptr);
+}
+
+namespace b200 {
+int op_dot_blocks(b200_op op, size_t *doubles) {
+  const b200_op_desc &d = op->d;
+  const bool ok = !op->jit && op->stage == kStagePTma && op->dot_grid > 0 && d.scatter != B200_SCATTER_DETERMINISTIC && d.num_elem > 0 &&
+                  d.qf != B200_QF_POISSON_KAPPA;
+  if (doubles) *doubles = ok ? (size_t)op->dot_grid : 0;
+  return ok ? op->dot_grid : 0;
+}
+int op_apply_dot(b200_op op, const void *u, void *v, const void *qdata, double *partial) {
+  B200_CHECK(partial && op_dot_blocks(op, nullptr) > 0, B200_ERROR_UNSUPPORTED, "op_apply_dot needs a persistent FP32 operator with the atomic scatter");
+  return op_apply_impl(op, u, v, qdata, nullptr, 0, partial);
+}
+}  // namespace b200
+
+extern "C" int b200_op_dot_len(b200_op op, int *blocks, int64_t *doubles) {
+  size_t    len = 0;
+  const int nb  = op_dot_blocks(op, &len);
+  if (blocks) *blocks = nb;
+  if (doubles) *doubles = (int64_t)len;
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_op_apply_dot(b200_op op, const void *u, void *v, const void *qdata, double *partial) {
+  return op_apply_dot(op, u, v, qdata, partial);
 }
 
 extern "C" int b200_op_kappa_grad(b200_op op, const void *u, const void *w, const void *qdata, void *g) {
@@ -542,6 +576,7 @@ extern "C" int b200_op_create_jit(b200_ctx ctx, const b200_op_desc *desc, const 
   op->stage           = 0;
   op->variant         = -1;
   op->grid            = 0;
+  op->dot_grid        = 0;
   *out                = op;
   return B200_SUCCESS;
 }
@@ -563,7 +598,9 @@ extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void 
     void          *v, *e_out;
     const void    *qdata, *kappa;
     int           *status;
-  } a{d.num_elem, d.comp_stride, op->epb, d.scatter == B200_SCATTER_DETERMINISTIC, d.offsets, u, v, op->e_work, nullptr, nullptr, ctx->d_status};
+    double        *dot;
+  } a{d.num_elem, d.comp_stride, op->epb, d.scatter == B200_SCATTER_DETERMINISTIC, d.offsets, u, v, op->e_work, nullptr, nullptr, ctx->d_status,
+      nullptr};
   static_assert(sizeof(ArgsBlob) == sizeof(OpArgs<double>), "argument layout");
   struct FieldsBlob {
     const void *passive[kJitMaxFieldsHost];

@@ -1,10 +1,12 @@
-// Deterministic two-pass reductions (sum of squares, |x| sum, max |x|, dot product), accumulated in FP64.
+// Deterministic two-pass reductions (sum of squares, |x| sum, max |x|, dot product); the per-block and final passes add
+// in FP64.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
+#include "b200_dfloat.cuh"
 #include "b200_internal.cuh"
 
 namespace b200 {
@@ -17,30 +19,14 @@ inline int reduce_blocks(int num_sms) { return 2 * num_sms; }
 
 __device__ __forceinline__ double red_combine(int kind, double a, double b) { return kind == kRedMaxAbs ? fmax(a, b) : a + b; }
 
-// Per-thread accumulators.  FP64 data: a double.  FP32 data: a float-float sum (~48 bits) on the FP32 pipe -- each
-// product's rounding error from an FMA (the product itself by __fmul_rn, so that it is not contracted into the sum)
-// and each addition's from Knuth's TwoSum, collected in the low word -- instead of converting every value to double,
-// which on this GPU puts two conversions and a multiply-add per element on the FP64 pipe (1/60 of the FP32 rate) and
-// bounded the FP32 CG's dot products at a fifth of the HBM rate.
+// Per-thread accumulators.  FP64 data: a double.  FP32 data: F2Acc (float-float on the FP32 pipe) instead of
+// converting every value to double, which on this GPU puts two conversions and a multiply-add per element on the FP64
+// pipe (1/60 of the FP32 rate) and bounded the FP32 CG's dot products at a fifth of the HBM rate.
 struct DAcc {
   double                            s = 0.0;
   __device__ __forceinline__ void   add(double v) { s += v; }
   __device__ __forceinline__ void   add_prod(double a, double b) { s += a * b; }
   __device__ __forceinline__ double value() const { return s; }
-};
-struct F2Acc {
-  float                           hi = 0.f, lo = 0.f;
-  __device__ __forceinline__ void add(float v) {
-    const float s = __fadd_rn(hi, v), bb = __fsub_rn(s, hi);
-    lo            = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
-    hi            = s;
-  }
-  __device__ __forceinline__ void add_prod(float a, float b) {
-    const float p = __fmul_rn(a, b);
-    lo            = __fadd_rn(lo, __fmaf_rn(a, b, -p));
-    add(p);
-  }
-  __device__ __forceinline__ double value() const { return isfinite(hi) ? (double)hi + (double)lo : (double)hi; }
 };
 template <typename T>
 struct AccFor {

@@ -11,11 +11,12 @@ from .ceed import F32, F64
 
 
 def cg_solve(ceed, op, qdata64, mask, b, x, mixed=False, op32=None, qdata32=None, rtol=1e-10, inner_rtol=1e-4, max_it=20000,
-             max_outer=30, use_graph=True, check_every=25, jacobi=None):
+             max_outer=30, use_graph=True, check_every=25, jacobi=None, fused_pdot=True):
     """Solve m A(m x) = m b from x = 0; returns a dict of iteration counts, final FP64 residual and device seconds.
-    jacobi: a Vector holding the masked inverse diagonal (see jacobi_preconditioner) for Jacobi-preconditioned CG."""
+    jacobi: a Vector holding the masked inverse diagonal (see jacobi_preconditioner) for Jacobi-preconditioned CG.
+    fused_pdot: in mixed mode, let a persistent FP32 operator sum p.(A p) during its apply (False: a separate pass)."""
     o = CGOpts(rtol, max_it, 1 if mixed else 0, inner_rtol, max_outer, 1 if use_graph else 0, check_every,
-               jacobi.data.data_ptr() if jacobi is not None else None)
+               jacobi.data.data_ptr() if jacobi is not None else None, 0 if fused_pdot else 1)
     s = CGStats()
     f64 = op.fused(op._kernel_prec(F64))  # F64X kernels when op.arithmetic == "float-float" (same double vectors)
     f32 = op32.fused(F32).h if mixed else None

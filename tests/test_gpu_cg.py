@@ -79,3 +79,61 @@ def test_graph_and_eager_agree(problem):
         cg_solve(ceed, o64["op"], o64["qdata"], mask, b, x, use_graph=graph, check_every=10, rtol=1e-8)
         xs.append(x.get_array_read())
     assert np.array_equal(xs[0], xs[1]) and np.array_equal(xs[1], xs[2])
+
+
+@pytest.mark.parametrize("qf", ["Poisson3DApply", "MassApply"])
+@pytest.mark.parametrize("n,degree,epb", [(3, 1, 4), (3, 3, 4), (4, 4, 6), (2, 6, 1), (2, 7, 1)])
+def test_apply_dot_matches_dot_of_output(qf, n, degree, epb):
+    """u . (A u) summed inside the persistent FP32 kernel equals the FP64 dot of u with the kernel's own output, and the
+    output equals the plain apply's.  27 elements in batches of 4 leave inactive teams in the last batch, and every case
+    launches more blocks than batches (blocks without a batch write 0)."""
+    ceed = lc.Ceed("/gpu/cuda/b200")
+    box = mesh.Box(n, degree, noise=0.05, seed=3)
+    o = build_poisson(ceed, box, dtype=torch.float32, qf_name=qf)
+    o["op"].fused(lc.F32).set_tile(epb, 7)
+    u = ceed.Vector(box.l_size, torch.float32)
+    u.set_array(mesh.uniform(17, box.l_size, -1.0, 1.0))
+    v, v_ref = ceed.Vector(box.l_size, torch.float32), ceed.Vector(box.l_size, torch.float32)
+    d = o["op"].apply_dot(u, v)
+    o["op"].apply(u, v_ref)
+    uh, vh, vr = u.get_array_read().astype(np.float64), v.get_array_read().astype(np.float64), v_ref.get_array_read()
+    assert np.allclose(vh, vr, rtol=1e-5, atol=1e-5 * np.abs(vr).max())
+    want = float(uh @ vh)
+    assert d > 0 and abs(d - want) <= 2e-5 * abs(want)
+
+
+def test_apply_dot_unavailable_without_persistent_kernel():
+    ceed = lc.Ceed("/gpu/cuda/b200")
+    box = mesh.Box(3, 3, noise=0.05, seed=3)
+    o = build_poisson(ceed, box, dtype=torch.float32)
+    o["op"].fused(lc.F32).set_tile(4, 5)
+    u, v = ceed.Vector(box.l_size, torch.float32), ceed.Vector(box.l_size, torch.float32)
+    u.set_value(1.0)
+    with pytest.raises(lc.B200Error):
+        o["op"].apply_dot(u, v)
+
+
+@pytest.mark.parametrize("jacobi", [False, True])
+def test_cg_fused_pdot_matches_separate(problem, jacobi):
+    """Mixed CG on the persistent FP32 kernel: p.(A p) summed inside the apply or in a separate pass over p and A p
+    gives the same convergence (iteration counts within a few) and the oracle-checked residual."""
+    from libceed_gb300.solver import jacobi_preconditioner
+
+    ceed, box, o64, o32, mask, b, m, bh, pb = problem
+    o32["op"].fused(lc.F32).set_tile(4, 7)
+    try:
+        pre = jacobi_preconditioner(ceed, o64["op"], mask) if jacobi else None
+        stats = {}
+        for fused in (True, False):
+            x = ceed.Vector(box.l_size)
+            st = cg_solve(ceed, o64["op"], o64["qdata"], mask, b, x, mixed=True, op32=o32["op"], qdata32=o32["qdata"], rtol=1e-10,
+                          check_every=10, jacobi=pre, fused_pdot=fused)
+            assert st["converged"] and st["rel_residual"] <= 1e-10
+            r = m * (bh - pb.apply(m * x.get_array_read()))
+            assert np.linalg.norm(r) / np.linalg.norm(bh) < 2e-10
+            stats[fused] = st
+        assert abs(stats[True]["iterations"] - stats[False]["iterations"]) <= max(5, stats[False]["iterations"] // 20)
+        # One kernel fewer per iteration (the pass over p and A p).
+        assert stats[True]["launches"] < stats[False]["launches"]
+    finally:
+        o32["op"].fused(lc.F32).set_tile(0, 0)
