@@ -87,3 +87,31 @@ def test_flops_estimate_matches_reference_model():
         assert out.value == int(g["flops"][0]), case
         checked += 1
     assert checked >= 10
+
+
+def test_struct_mirrors_match_the_header(tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's field offsets and sizes."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "ceed-b200.h"', "int main(void) {"]
+    want = {}
+    for cname, py in _ffi._STRUCTS.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        want[(cname, "sizeof")] = ctypes.sizeof(py)
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+            want[(cname, fname)] = getattr(py, fname).offset
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        s, f, v = line.split()
+        got[(s, f)] = int(v)
+    assert got == want
