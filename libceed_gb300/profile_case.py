@@ -1,6 +1,6 @@
 """A small, self-contained fused-apply case for profilers (ncu) and quick timing.
 
-    python -m libceed_gb300.profile_case --degree 4 --prec f64 --n 32 --reps 3 [--det] [--epb E --staging S]
+    python -m libceed_gb300.profile_case --degree 4 --prec f64 --n 32 --reps 3 [--det] [--epb E --staging S] [--dot]
 
 --prec f64x runs the float-float kernels on the same double vectors.
 
@@ -28,6 +28,7 @@ def main():
     ap.add_argument("--epb", type=int, default=0)
     ap.add_argument("--staging", type=int, default=0)
     ap.add_argument("--cg", action="store_true", help="time the FP64 and FP32-refined CG solves of the box instead")
+    ap.add_argument("--dot", action="store_true", help="time apply_dot (v = A u and u . A u, persistent FP32 kernel) instead")
     a = ap.parse_args()
     if a.cg:
         return cg_case(a)
@@ -43,18 +44,30 @@ def main():
     u = ceed.Vector(box.l_size, dt)
     u.set_array(box.u())
     v = ceed.Vector(box.l_size, dt)
-    op.apply(u, v)
+    run = lambda: op.apply(u, v)  # noqa: E731
+    if a.dot:
+        import ctypes
+
+        from libceed_gb300._ffi import call
+
+        f32 = op.fused(lc.F32)
+        nb, nd = ctypes.c_int(), ctypes.c_int64()
+        call("b200_op_dot_len", f32.h, ctypes.byref(nb), ctypes.byref(nd))
+        part = torch.empty(max(nd.value, 1), dtype=torch.float64, device=ceed.device)
+        qd = objs["qdata"]
+        run = lambda: call("b200_op_apply_dot", f32.h, u.ptr(), v.ptr(), qd.ptr(), ctypes.c_void_p(part.data_ptr()))  # noqa: E731
+    run()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(a.reps):
-        op.apply(u, v)
+        run()
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / a.reps
     fused = op.fused({"f64": lc.F64, "f32": lc.F32, "f64x": lc.F64X}[a.prec])
     b, f = fused.cost()
-    print(f"degree {a.degree} {a.prec} n={a.n} dof={box.l_size} tile={fused.tile()} {ms:.4f} ms/apply "
+    print(f"degree {a.degree} {a.prec} n={a.n}{' apply_dot' if a.dot else ''} dof={box.l_size} tile={fused.tile()} {ms:.4f} ms/apply "
           f"{box.l_size / ms / 1e6:.3f} GDoF/s {b / ms / 1e6:.1f} GB/s(alg) {f / ms / 1e9:.3f} TFLOP/s alg_bytes={b:.0f}")
 
 
