@@ -103,6 +103,14 @@ int b200_vec_norm(b200_ctx ctx, int prec, int64_t n, const void *x, int norm_typ
 int b200_vec_dot(b200_ctx ctx, int prec, int64_t n, const void *x, const void *y, double *dot);
 int b200_vec_convert(b200_ctx ctx, int64_t n, int src_prec, const void *src, int dst_prec, void *dst);
 
+/* ---- Strided vector access.  Replaces CeedVectorSetValueStrided / CeedVectorCopyStrided
+ *      (interface/ceed-vector.c:412, :300) and their device kernels setValueStridedK / copyStridedK
+ *      (backends/cuda-ref/kernels/cuda-ref-vector.cu:14-80): entries start, start + step, ... below stop, with
+ *      stop = -1 meaning `length` (for the copy, the shorter of the two vectors' lengths).  stop outside [-1, length],
+ *      start outside [0, stop] or step <= 0 return B200_ERROR_ACCESS before anything runs. */
+int b200_vec_set_value_strided(b200_ctx ctx, int prec, int64_t length, int64_t start, int64_t stop, int64_t step, void *x, double value);
+int b200_vec_copy_strided(b200_ctx ctx, int prec, int64_t length, int64_t start, int64_t stop, int64_t step, const void *x, void *y);
+
 /* ---- Element restriction.  Offset form replaces OffsetNoTranspose / OffsetTranspose
  *      (include/ceed/jit-source/cuda/cuda-ref-restriction-offset.h:15-67, host side
  *      backends/cuda-ref/ceed-cuda-ref-restriction.c); strided form replaces cuda-ref-restriction-strided.h.

@@ -201,6 +201,39 @@ static int CeedVectorSetValue_B200(CeedVector vec, CeedScalar value) {
   return CEED_ERROR_SUCCESS;
 }
 
+// Strided set and copy keep the entries outside the range, so the vector must hold data already (as
+// backends/cuda-ref/ceed-cuda-ref-vector.c:243-375 requires); stop = -1 is resolved by b200_vec_*_strided.
+static int CeedVectorSetValueStrided_B200(CeedVector vec, CeedSize start, CeedSize stop, CeedSize step, CeedScalar value) {
+  CeedVector_B200  *impl;
+  b200_ctx          ctx;
+  CeedSize          n;
+  const CeedScalar *d;
+
+  CeedCallBackend(VecData(vec, &impl, &ctx, &n));
+  CeedCheck(impl->h_valid || impl->d_valid, CeedVectorReturnCeed(vec), CEED_ERROR_BACKEND, "CeedVector must have valid data set");
+  CeedCallBackend(CeedVectorGetDevice_B200(vec, true, &d));
+  CeedCallB200(CeedVectorReturnCeed(vec), b200_vec_set_value_strided(ctx, B200_F64, n, start, stop, step, (void *)d, value));
+  return CEED_ERROR_SUCCESS;
+}
+
+static int CeedVectorCopyStrided_B200(CeedVector vec, CeedSize start, CeedSize stop, CeedSize step, CeedVector vec_copy) {
+  CeedVector_B200  *impl, *impl_copy;
+  b200_ctx          ctx;
+  CeedSize          n, n_copy;
+  const CeedScalar *dx, *dy;
+
+  CeedCallBackend(VecData(vec, &impl, &ctx, &n));
+  CeedCallBackend(CeedVectorGetData(vec_copy, &impl_copy));
+  CeedCallBackend(CeedVectorGetLength(vec_copy, &n_copy));
+  CeedCheck(impl->h_valid || impl->d_valid, CeedVectorReturnCeed(vec), CEED_ERROR_BACKEND, "CeedVector must have valid data set");
+  CeedCheck(impl_copy->h_valid || impl_copy->d_valid, CeedVectorReturnCeed(vec_copy), CEED_ERROR_BACKEND,
+            "CeedVector must have valid data set");
+  CeedCallBackend(CeedVectorGetDevice_B200(vec, false, &dx));
+  CeedCallBackend(CeedVectorGetDevice_B200(vec_copy, true, &dy));
+  CeedCallB200(CeedVectorReturnCeed(vec), b200_vec_copy_strided(ctx, B200_F64, n < n_copy ? n : n_copy, start, stop, step, dx, (void *)dy));
+  return CEED_ERROR_SUCCESS;
+}
+
 static int CeedVectorNorm_B200(CeedVector vec, CeedNormType type, CeedScalar *norm) {
   CeedVector_B200  *impl;
   b200_ctx          ctx;
@@ -307,6 +340,8 @@ int CeedVectorCreate_B200(CeedSize n, CeedVector vec) {
   CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "RestoreArray", CeedVectorRestoreArray_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "RestoreArrayRead", CeedVectorRestoreArrayRead_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "SetValue", CeedVectorSetValue_B200));
+  CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "SetValueStrided", CeedVectorSetValueStrided_B200));
+  CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "CopyStrided", CeedVectorCopyStrided_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "Norm", CeedVectorNorm_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "Scale", CeedVectorScale_B200));
   CeedCallBackend(CeedSetBackendFunction(ceed, "Vector", vec, "AXPY", CeedVectorAXPY_B200));

@@ -210,6 +210,19 @@ class Vector:
     def set_value(self, value):
         call("b200_vec_set_value", self.ceed._ctx, self.prec, self.size, self.ptr(), float(value))
 
+    def set_value_strided(self, start, stop, step, value):
+        """Entries start, start + step, ... below stop (-1: the length) set to value (CeedVectorSetValueStrided)."""
+        call("b200_vec_set_value_strided", self.ceed._ctx, self.prec, self.size, int(start), int(stop), int(step), self.ptr(),
+             float(value))
+
+    def copy_strided(self, start, stop, step, vec_copy):
+        """vec_copy[i] = self[i] for i = start, start + step, ... below stop (-1: the shorter length)
+        (CeedVectorCopyStrided); both vectors hold the same scalar type."""
+        if vec_copy.dtype != self.dtype:
+            raise B200Error("CeedVectorCopyStrided", 4, f"copy from {self.dtype} into {vec_copy.dtype}")
+        call("b200_vec_copy_strided", self.ceed._ctx, self.prec, min(self.size, vec_copy.size), int(start), int(stop), int(step),
+             self.ptr(), vec_copy.ptr())
+
     def norm(self, normtype=NORM_2):
         out = ctypes.c_double()
         call("b200_vec_norm", self.ceed._ctx, self.prec, self.size, self.ptr(), normtype, ctypes.byref(out))

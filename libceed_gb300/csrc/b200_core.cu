@@ -56,6 +56,19 @@ __global__ void k_reciprocal(int64_t n, T *__restrict__ x) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     if (fabs((double)x[i]) > 1e-16) x[i] = (T)1 / x[i];  // as rcpValueK: entries below CEED_EPSILON are left alone
 }
+// Strided forms: entry start + j * step for j < count (count already clipped to the range on the host).
+template <typename T>
+__global__ void k_set_value_strided(int64_t count, int64_t start, int64_t step, T *__restrict__ x, T value) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x)
+    x[start + j * step] = value;
+}
+template <typename T>
+__global__ void k_copy_strided(int64_t count, int64_t start, int64_t step, const T *__restrict__ x, T *__restrict__ y) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = start + j * step;
+    y[i]            = x[i];
+  }
+}
 template <typename S, typename D>
 __global__ void k_convert(int64_t n, const S *__restrict__ src, D *__restrict__ dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) dst[i] = (D)src[i];
@@ -218,6 +231,49 @@ extern "C" int b200_vec_reciprocal(b200_ctx ctx, int prec, int64_t n, void *x) {
   B200_PREC_DISPATCH(prec, T, {
     k_reciprocal<T><<<stride_grid(ctx, n, 256), 256, 0, ctx->stream>>>(n, (T *)x);
     B200_LAUNCHED(ctx, "reciprocal");
+  });
+  return B200_SUCCESS;
+}
+
+// Checks the range of the strided forms as CeedVectorCopyStrided / CeedVectorSetValueStrided do
+// (interface/ceed-vector.c:300-325, :412-425): stop in [-1, length] with -1 meaning length, start in [0, length] and
+// not past stop (CEED_ERROR_ACCESS otherwise); step must be positive (the reference's host loop never ends for
+// step <= 0).  *count is the number of entries start, start + step, ... below stop.
+static int strided_count(const char *who, int64_t length, int64_t start, int64_t stop, int64_t step, int64_t *count) {
+  *count = 0;
+  B200_CHECK(length >= 0, B200_ERROR_DIMENSION, "%s: negative length %lld", who, (long long)length);
+  B200_CHECK(stop >= -1 && stop <= length, B200_ERROR_ACCESS, "%s: invalid value for stop %lld, must be in the range [-1, %lld]", who,
+             (long long)stop, (long long)length);
+  if (stop == -1) stop = length;
+  B200_CHECK(start >= 0 && start <= stop, B200_ERROR_ACCESS, "%s: invalid value for start %lld, must be in the range [0, %lld]", who,
+             (long long)start, (long long)stop);
+  B200_CHECK(step > 0, B200_ERROR_ACCESS, "%s: step %lld must be positive", who, (long long)step);
+  *count = ceil_div(stop - start, step);
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_vec_set_value_strided(b200_ctx ctx, int prec, int64_t length, int64_t start, int64_t stop, int64_t step, void *x,
+                                          double value) {
+  int64_t count = 0;
+  int     st    = strided_count("b200_vec_set_value_strided", length, start, stop, step, &count);
+  if (st) return st;
+  if (count == 0) return B200_SUCCESS;
+  B200_PREC_DISPATCH(prec, T, {
+    k_set_value_strided<T><<<stride_grid(ctx, count, 256), 256, 0, ctx->stream>>>(count, start, step, (T *)x, (T)value);
+    B200_LAUNCHED(ctx, "set_value_strided");
+  });
+  return B200_SUCCESS;
+}
+
+extern "C" int b200_vec_copy_strided(b200_ctx ctx, int prec, int64_t length, int64_t start, int64_t stop, int64_t step, const void *x,
+                                     void *y) {
+  int64_t count = 0;
+  int     st    = strided_count("b200_vec_copy_strided", length, start, stop, step, &count);
+  if (st) return st;
+  if (count == 0) return B200_SUCCESS;
+  B200_PREC_DISPATCH(prec, T, {
+    k_copy_strided<T><<<stride_grid(ctx, count, 256), 256, 0, ctx->stream>>>(count, start, step, (const T *)x, (T *)y);
+    B200_LAUNCHED(ctx, "copy_strided");
   });
   return B200_SUCCESS;
 }

@@ -115,3 +115,19 @@ def test_struct_mirrors_match_the_header(tmp_path):
         s, f, v = line.split()
         got[(s, f)] = int(v)
     assert got == want
+
+
+@pytest.mark.parametrize("name", ["b200_vec_set_value_strided", "b200_vec_copy_strided"])
+def test_strided_range_checks_on_the_host(lib, name):
+    """The strided entry points check the range as CeedVectorSetValueStrided / CopyStrided do
+    (interface/ceed-vector.c:300-325, :412-425) before touching the context or a device pointer, so a null context
+    serves here: bad ranges give B200_ERROR_ACCESS (5), an empty range succeeds without a launch."""
+    fn = getattr(lib, name)
+    tail = (None, 1.0) if name == "b200_vec_set_value_strided" else (None, None)
+    n = 100
+    for start, stop, step in [(0, n + 1, 1), (0, -2, 1), (-1, -1, 1), (10, 5, 1), (0, -1, 0), (0, -1, -4)]:
+        assert fn(None, 0, n, start, stop, step, *tail) == 5, (start, stop, step)
+        assert "must be" in lib.b200_last_error().decode()
+    assert fn(None, 0, -1, 0, -1, 1, *tail) == 2  # negative length: B200_ERROR_DIMENSION
+    for start, stop in [(7, 7), (n, -1), (0, 0)]:
+        assert fn(None, 0, n, start, stop, 3, *tail) == 0

@@ -46,6 +46,42 @@ def test_vector_ops(ceed, dtype):
     assert len({x.norm() for _ in range(5)}) == 1
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("start,stop,step", [(0, -1, 1), (3, -1, 7), (5, 1000, 3), (17, 17, 2), (0, 4099, 4099), (4098, -1, 1),
+                                             (2, -1, 10**12)])
+def test_vector_strided(ceed, dtype, start, stop, step):
+    """CeedVectorSetValueStrided / CopyStrided (interface/ceed-vector.c:300, :412): exactly the entries
+    start, start + step, ... below stop change; stop = -1 means the length (the shorter one for the copy)."""
+    n = 4099
+    x0, y0 = lc.mesh.uniform(3, n), lc.mesh.uniform(4, n + 5)
+    x, y = ceed.Vector(n, dtype), ceed.Vector(n + 5, dtype)
+    x.set_array(x0)
+    y.set_array(y0)
+    xs, ys = x.get_array_read().copy(), y.get_array_read().copy()
+    end = n if stop == -1 else stop
+    want = xs.copy()
+    want[start:end:step] = -2.5
+    x.set_value_strided(start, stop, step, -2.5)
+    assert np.array_equal(x.get_array_read(), want)
+    want_y = ys.copy()
+    want_y[start:end:step] = want[start:end:step]
+    x.copy_strided(start, stop, step, y)
+    assert np.array_equal(y.get_array_read(), want_y)
+
+
+def test_vector_strided_rejects_bad_ranges(ceed):
+    """Out-of-range stop or start and a non-positive step are refused before any kernel runs, vector unchanged."""
+    n = 64
+    x = ceed.Vector(n)
+    x.set_value(1.0)
+    for start, stop, step in [(0, n + 1, 1), (0, -2, 1), (-1, -1, 1), (10, 5, 1), (0, -1, 0), (0, -1, -3)]:
+        with pytest.raises(lc.B200Error):
+            x.set_value_strided(start, stop, step, 7.0)
+        with pytest.raises(lc.B200Error):
+            x.copy_strided(start, stop, step, ceed.Vector(n))
+    assert np.all(x.get_array_read() == 1.0)
+
+
 def test_empty_vectors(ceed):
     v = ceed.Vector(0)
     v.set_value(1.0)
