@@ -93,6 +93,30 @@ class Box:
     def u(self, seed=None):
         return uniform(self.seed + 1 if seed is None else seed, self.l_size)
 
+    def node_coords(self):
+        """Physical (x, y, z) of every solution node, shape [num_nodes, 3] in L-vector node order: the trilinear map
+        of each element's 8 vertices evaluated at its Gauss-Lobatto nodes (the coordinate field that Poisson3DBuild and
+        Mass3DBuild see; neighbouring elements agree on shared nodes because the map is conforming)."""
+        from .basis1d import lobatto_quadrature
+
+        n, p = self.n, self.degree
+        nd, nv1 = n * p + 1, n + 1
+        gll, _ = lobatto_quadrature(p + 1)
+        lat = np.arange(nd)
+        elem = np.minimum(lat // p, n - 1)                     # element along one direction; the last node stays in n - 1
+        t = 0.5 * (gll[lat - elem * p] + 1.0)                  # reference coordinate in [0, 1] inside that element
+        X = self.coords().reshape(3, nv1, nv1, nv1)            # [c][k][j][i]
+        out = np.zeros((3, nd, nd, nd))
+        for dk in (0, 1):
+            wz = (t if dk else 1.0 - t)[:, None, None]
+            for dj in (0, 1):
+                wy = (t if dj else 1.0 - t)[None, :, None]
+                for di in (0, 1):
+                    wx = (t if di else 1.0 - t)[None, None, :]
+                    corner = X[:, (elem + dk)[:, None, None], (elem + dj)[None, :, None], (elem + di)[None, None, :]]
+                    out += wz * wy * wx * corner
+        return np.ascontiguousarray(out.reshape(3, -1).T)
+
 
 def node_lattice(n, degree):
     """Reference (unperturbed) coordinates in [0,1] of the 1D node lattice: element k's Gauss-Lobatto nodes."""

@@ -10,6 +10,7 @@ import os
 import numpy as np
 import pytest
 
+from libceed_gb300 import mesh
 from oracle import oracle as orc
 from tests.conftest import GOLDEN, relinf
 
@@ -125,3 +126,34 @@ def test_poisson_constant_nullspace():
     pb = orc.BoxProblem(3, 4, poisson=True, seed=7)
     v = pb.apply(np.ones(pb.l_size))
     assert np.max(np.abs(v)) < 1e-13
+
+
+@pytest.mark.parametrize("n,p", [(3, 1), (3, 3), (2, 5), (4, 2)])
+def test_volume_known_answer(n, p):
+    """1^T M 1 is the volume of the domain (examples/ceed/ex1-volume.c:262-272; exact volume 1 for the unit box, whose
+    boundary vertices are never perturbed).  Gauss points Q = P + 1 integrate the trilinear map's det J exactly, so
+    the bound is rounding, far inside ex1's 1e-5."""
+    pb = orc.BoxProblem(n, p, poisson=False, noise=0.1, seed=70 + p)
+    assert abs(pb.apply(np.ones(pb.l_size)).sum() - 1.0) < 1e-13
+
+
+def test_surface_known_answer():
+    """sum |A (x + y + z)| is the surface area (examples/ceed/ex2-surface.c:248-290), 6 for the unit box, within
+    ex2's 3D tolerance of 1e-1; edge nodes between faces of opposite normal sign cancel, so the gap shrinks with h."""
+    box = mesh.Box(8, 4, noise=0.05, seed=71)
+    pb = orc.BoxProblem(8, 4, poisson=True, noise=0.05, seed=71)
+    v = pb.apply(box.node_coords().sum(axis=1))
+    assert abs(np.abs(v).sum() - 6.0) < 1e-1
+
+
+@pytest.mark.parametrize("n,p", [(3, 1), (3, 3), (2, 5)])
+def test_linear_fields_energy_identity(n, p):
+    """For fields linear in physical space (exactly representable on the trilinear mesh), a^T A b = grad a . grad b
+    times the volume: (x+y+z)^T A (x+y+z) = 3, x^T A y = 0.  Exact up to rounding, so it pins the node coordinates
+    and the Poisson qdata together."""
+    box = mesh.Box(n, p, noise=0.05, seed=72)
+    pb = orc.BoxProblem(n, p, poisson=True, noise=0.05, seed=72)
+    xyz = box.node_coords()
+    s = xyz.sum(axis=1)
+    assert abs(s @ pb.apply(s) - 3.0) < 1e-12
+    assert abs(xyz[:, 0] @ pb.apply(xyz[:, 1])) < 1e-12
