@@ -130,10 +130,14 @@ extern "C" int b200_basis_create(b200_ctx ctx, int dim, int P_1d, int Q_1d, int 
   std::vector<float> hf(h.begin(), h.end());
   b200_basis         b = new b200_basis_s();
   b->ctx = ctx, b->dim = dim, b->P = P_1d, b->Q = Q_1d, b->num_comp = num_comp;
-  B200_CUDA(cudaMalloc(&b->mats_f64, sizeof(double) * n));
-  B200_CUDA(cudaMalloc(&b->mats_f32, sizeof(float) * n));
-  B200_CUDA(cudaMemcpy(b->mats_f64, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-  B200_CUDA(cudaMemcpy(b->mats_f32, hf.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+  cudaError_t err = cudaMalloc(&b->mats_f64, sizeof(double) * n);  // b is value-initialised: a partial basis frees cleanly
+  if (err == cudaSuccess) err = cudaMalloc(&b->mats_f32, sizeof(float) * n);
+  if (err == cudaSuccess) err = cudaMemcpy(b->mats_f64, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(b->mats_f32, hf.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    b200_basis_destroy(b);
+    return cuda_status(err, "b200_basis_create", __FILE__, __LINE__);
+  }
   *out = b;
   return B200_SUCCESS;
 }

@@ -98,10 +98,14 @@ extern "C" int b200_ctx_create(int device_id, b200_ctx *out) {
   ctx->stream   = 0;
   ctx->launches = 0;
   ctx->red_blocks = reduce_blocks(ctx->num_sms);
-  B200_CUDA(cudaMalloc(&ctx->red_partial, sizeof(double) * (size_t)(2 * ctx->red_blocks + 8)));
-  B200_CUDA(cudaMallocHost(&ctx->red_result_host, sizeof(double) * 8));
-  B200_CUDA(cudaMalloc(&ctx->d_status, sizeof(int)));
-  B200_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
+  cudaError_t err = cudaMalloc(&ctx->red_partial, sizeof(double) * (size_t)(2 * ctx->red_blocks + 8));  // pointers start null
+  if (err == cudaSuccess) err = cudaMallocHost(&ctx->red_result_host, sizeof(double) * 8);
+  if (err == cudaSuccess) err = cudaMalloc(&ctx->d_status, sizeof(int));
+  if (err == cudaSuccess) err = cudaMemset(ctx->d_status, 0, sizeof(int));
+  if (err != cudaSuccess) {
+    b200_ctx_destroy(ctx);
+    return cuda_status(err, "b200_ctx_create", __FILE__, __LINE__);
+  }
   *out = ctx;
   return B200_SUCCESS;
 }

@@ -161,25 +161,30 @@ extern "C" int b200_plan_create(b200_ctx ctx, int64_t num_elem, int elem_size, i
   std::vector<int32_t> t_idx((size_t)n);
   for (int64_t i = 0; i < n; i++) t_idx[(size_t)pos[(size_t)offsets_host[i]]++] = (int32_t)i;
 
-  b200_plan p   = new b200_plan_s();
-  p->ctx        = ctx;
-  p->num_elem   = num_elem;
-  p->elem_size  = elem_size;
+  B200_CHECK((int64_t)max_off + (int64_t)(num_comp - 1) * comp_stride < l_size, B200_ERROR_DIMENSION,
+             "offsets reach %lld, beyond the L-vector length %lld", (long long)max_off + (long long)(num_comp - 1) * comp_stride, (long long)l_size);
+
+  b200_plan p    = new b200_plan_s();  // value-initialised: device pointers start null, so b200_plan_destroy frees a partial plan
+  p->ctx         = ctx;
+  p->num_elem    = num_elem;
+  p->elem_size   = elem_size;
   p->num_unique  = (int64_t)l_idx.size();
   p->num_comp    = num_comp;
   p->comp_stride = comp_stride;
   p->l_size      = l_size;
-  B200_CHECK((int64_t)max_off + (int64_t)(num_comp - 1) * comp_stride < l_size, B200_ERROR_DIMENSION,
-             "offsets reach %lld, beyond the L-vector length %lld", (long long)max_off + (long long)(num_comp - 1) * comp_stride, (long long)l_size);
   // A valid restriction maps distinct (offset, component) pairs to distinct entries, so it writes every entry of the
   // L-vector exactly when the pairs are as many as the entries.
-  p->covers_all = p->num_unique * num_comp == l_size;
-  B200_CUDA(cudaMalloc(&p->l_indices, sizeof(int32_t) * l_idx.size()));
-  B200_CUDA(cudaMalloc(&p->t_start, sizeof(int32_t) * t_start.size()));
-  B200_CUDA(cudaMalloc(&p->t_indices, sizeof(int32_t) * t_idx.size()));
-  B200_CUDA(cudaMemcpy(p->l_indices, l_idx.data(), sizeof(int32_t) * l_idx.size(), cudaMemcpyHostToDevice));
-  B200_CUDA(cudaMemcpy(p->t_start, t_start.data(), sizeof(int32_t) * t_start.size(), cudaMemcpyHostToDevice));
-  B200_CUDA(cudaMemcpy(p->t_indices, t_idx.data(), sizeof(int32_t) * t_idx.size(), cudaMemcpyHostToDevice));
+  p->covers_all  = p->num_unique * num_comp == l_size;
+  cudaError_t err = cudaMalloc(&p->l_indices, sizeof(int32_t) * l_idx.size());
+  if (err == cudaSuccess) err = cudaMalloc(&p->t_start, sizeof(int32_t) * t_start.size());
+  if (err == cudaSuccess) err = cudaMalloc(&p->t_indices, sizeof(int32_t) * t_idx.size());
+  if (err == cudaSuccess) err = cudaMemcpy(p->l_indices, l_idx.data(), sizeof(int32_t) * l_idx.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(p->t_start, t_start.data(), sizeof(int32_t) * t_start.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(p->t_indices, t_idx.data(), sizeof(int32_t) * t_idx.size(), cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    b200_plan_destroy(p);
+    return cuda_status(err, "b200_plan_create", __FILE__, __LINE__);
+  }
   *out = p;
   return B200_SUCCESS;
 }
