@@ -249,6 +249,7 @@ struct CgWork {
   double  *r64, *p64, *w64, *z64;
   float   *x32, *r32, *p32, *w32, *z32, *mask32, *inv32;
   const double *inv64;  // Jacobi preconditioner (masked 1/diag) or nullptr
+  cudaEvent_t   e0, e1;  // device time of the solve
 };
 
 template <typename T>
@@ -307,27 +308,34 @@ static int cg_loop(CgWork &wk, b200_op op, const void *qdata, const T *mask, T *
     const int count = every < max_it - done ? every : max_it - done;
     if (use_graph && count == every) {
       if (!exec) {
-        cudaGraph_t   graph;
-        const int64_t l0 = ctx->launches;
-        B200_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, z, inv, count);
-        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-        if (st) return st;
-        B200_CUDA(ce);
-        B200_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-        B200_CUDA(cudaGraphDestroy(graph));
+        // Failures below leave the loop with st set, so the graph and its executable are always destroyed.
+        cudaGraph_t     graph = nullptr;
+        cudaGraphExec_t ge    = nullptr;
+        const int64_t   l0    = ctx->launches;
+        st = cuda_status(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture", __FILE__, __LINE__);
+        if (st) break;
+        st                = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, z, inv, count);
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (!st) st = cuda_status(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+        if (!st) st = cuda_status(cudaGraphInstantiate(&ge, graph, 0), "cudaGraphInstantiate", __FILE__, __LINE__);
+        if (graph) cudaGraphDestroy(graph);
+        if (st) break;
+        exec          = ge;
         per_graph     = ctx->launches - l0;
         ctx->launches = l0;  // captured, not yet run
       }
-      B200_CUDA(cudaGraphLaunch(exec, ctx->stream));
+      st = cuda_status(cudaGraphLaunch(exec, ctx->stream), "cudaGraphLaunch", __FILE__, __LINE__);
+      if (st) break;
       ctx->launches += per_graph;
     } else {
       st = cg_iterations<T>(wk, op, qdata, mask, x, r, p, w, z, inv, count);
       if (st) break;
     }
     done += count;
-    B200_CUDA(cudaMemcpyAsync(wk.s_host, wk.s + conv, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    B200_CUDA(cudaStreamSynchronize(ctx->stream));
+    st = cuda_status(cudaMemcpyAsync(wk.s_host, wk.s + conv, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync", __FILE__,
+                     __LINE__);
+    if (!st) st = cuda_status(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize", __FILE__, __LINE__);
+    if (st) break;
     rr = wk.s_host[0];
     if (!std::isfinite(rr)) {
       set_error("CG diverged (r.r = %g after %d iterations)", rr, done);
@@ -403,9 +411,9 @@ extern "C" int b200_cg_solve(b200_ctx ctx, b200_op op64, b200_op op32, const voi
   return st_solve;
 }
 
-static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask,
-                              const double *b, double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats) {
-  CgWork wk{};
+// The solve proper; every array and event it creates is recorded in wk, which the caller releases on every path.
+static int cg_run(CgWork &wk, b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask,
+                  const double *b, double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats) {
   wk.ctx    = ctx;
   wk.n      = n;
   wk.blocks = reduce_blocks(ctx->num_sms);
@@ -447,10 +455,9 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
     bnorm = sqrt(wk.s_host[0]);
   }
   const int64_t launches0 = ctx->launches;
-  cudaEvent_t   e0, e1;
-  B200_CUDA(cudaEventCreate(&e0));
-  B200_CUDA(cudaEventCreate(&e1));
-  B200_CUDA(cudaEventRecord(e0, ctx->stream));
+  B200_CUDA(cudaEventCreate(&wk.e0));
+  B200_CUDA(cudaEventCreate(&wk.e1));
+  B200_CUDA(cudaEventRecord(wk.e0, ctx->stream));
   const double target = opts->rtol * bnorm;
   double       rnorm  = 0.0;
   int          total  = 0;
@@ -493,18 +500,26 @@ static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const vo
     stats->outer = outer;
   }
   if (!st) {
-    B200_CUDA(cudaEventRecord(e1, ctx->stream));
-    B200_CUDA(cudaEventSynchronize(e1));
+    B200_CUDA(cudaEventRecord(wk.e1, ctx->stream));
+    B200_CUDA(cudaEventSynchronize(wk.e1));
     float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventElapsedTime(&ms, wk.e0, wk.e1);
     stats->seconds = ms * 1e-3;
   }
   stats->iterations   = total;
   stats->rel_residual = bnorm > 0 ? rnorm / bnorm : rnorm;
   stats->converged    = !st && rnorm <= target;
   stats->launches     = ctx->launches - launches0;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  return st;
+}
+
+static int cg_solve_on_stream(b200_ctx ctx, b200_op op64, b200_op op32, const void *qdata64, const void *qdata32, const double *mask,
+                              const double *b, double *x, int64_t n, const b200_cg_opts *opts, b200_cg_stats *stats) {
+  CgWork    wk{};
+  const int st = cg_run(wk, ctx, op64, op32, qdata64, qdata32, mask, b, x, n, opts, stats);
+  cudaStreamSynchronize(ctx->stream);  // nothing queued may still use the arrays freed below
+  if (wk.e0) cudaEventDestroy(wk.e0);
+  if (wk.e1) cudaEventDestroy(wk.e1);
   cudaFree(wk.partial);
   cudaFree(wk.partial2);
   cudaFree(wk.dot_partial);
