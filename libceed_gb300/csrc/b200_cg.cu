@@ -213,9 +213,10 @@ __global__ void __launch_bounds__(kReduceThreads) k_residual(int64_t n, const do
   if (threadIdx.x == 0) partial[blockIdx.x] = acc;
 }
 
-// Start of a CG solve: x = 0, r = p = rhs (masked already), and s[kRR] = s[kRRNew] = r.r.
+// Start of a CG solve: x = 0, r = p = rhs (masked already), and s[kRR] = s[kRRNew] = r.r.  rhs may be r itself (the
+// FP64 start scales r in place), so neither is __restrict__.
 template <typename T, typename S>
-__global__ void k_cg_start(int64_t n, const S *__restrict__ rhs, double scale, T *__restrict__ x, T *__restrict__ r, T *__restrict__ p) {
+__global__ void k_cg_start(int64_t n, const S *rhs, double scale, T *__restrict__ x, T *r, T *__restrict__ p) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const T v = (T)((double)rhs[i] * scale);
     x[i]      = 0;

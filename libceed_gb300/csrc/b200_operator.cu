@@ -609,7 +609,7 @@ extern "C" int b200_op_apply_jit(b200_op op, const void *u, void *v, const void 
   for (int i = 0; i < op->jit_num_passive && i < kJitMaxFieldsHost; i++) f.passive[i] = passive ? passive[i] : nullptr;
   f.ctx                 = qf_ctx;
   void        *params[] = {&a, &f, op->jit_mats.data()};
-  const int    Q = d.Q_1d, Q3 = Q * Q * Q;
+  const int    Q        = d.Q_1d;
   const size_t smem     = tsz * (size_t)op->epb * tile_team_stride(Q, 0);
   if (smem > 48 * 1024) B200_CUDA(cudaFuncSetAttribute((const void *)op->jit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int64_t grid = ceil_div(d.num_elem, op->epb);
