@@ -4,7 +4,8 @@
 //      and its assembled diagonal (CeedOperatorLinearAssembleDiagonal);
 //      the same with the resource option ":arithmetic=float-float" (float-float kernels on double vectors);
 //   2. gallery Mass3DBuild + the user QFunction ScaledMass from tests/qfunctions/user-qfunctions.h with a context
-//      (NVRTC-compiled on /gpu/cuda/b200, the function pointer on the CPU backend).
+//      (NVRTC-compiled on /gpu/cuda/b200, the function pointer on the CPU backend);
+//   3. CeedVectorSetValueStrided and CeedVectorCopyStrided (device kernels on /gpu/cuda/b200), compared bitwise.
 // Needs a GPU and a libCEED build; prints nothing on success, like the reference's tests/t*.c.
 #include <ceed.h>
 #include <math.h>
@@ -146,6 +147,30 @@ static void Apply(const char *resource, int n, int P, const double *coords, cons
   CeedDestroy(&ceed);
 }
 
+// x = u, then x[3:N:7] = -2.5, then y = 0 with y[1:-1:5] = x[1:-1:5]; returns x followed by y in out[2N].
+static void Strided(const char *resource, int N, const double *u, double *out) {
+  Ceed       ceed;
+  CeedVector x, y;
+
+  CeedInit(resource, &ceed);
+  CeedVectorCreate(ceed, N, &x);
+  CeedVectorCreate(ceed, N, &y);
+  CeedVectorSetArray(x, CEED_MEM_HOST, CEED_COPY_VALUES, (double *)u);
+  CeedVectorSetValue(y, 0.0);
+  CeedVectorSetValueStrided(x, 3, N, 7, -2.5);
+  CeedVectorCopyStrided(x, 1, -1, 5, y);
+  const double *a;
+  CeedVectorGetArrayRead(x, CEED_MEM_HOST, &a);
+  for (int i = 0; i < N; i++) out[i] = a[i];
+  CeedVectorRestoreArrayRead(x, &a);
+  CeedVectorGetArrayRead(y, CEED_MEM_HOST, &a);
+  for (int i = 0; i < N; i++) out[N + i] = a[i];
+  CeedVectorRestoreArrayRead(y, &a);
+  CeedVectorDestroy(&x);
+  CeedVectorDestroy(&y);
+  CeedDestroy(&ceed);
+}
+
 int main(void) {
   const int n = 3, P = 5, nv = (n + 1) * (n + 1) * (n + 1), nd = n * (P - 1) + 1, N = nd * nd * nd, ne = n * n * n;
   double   *coords = malloc(sizeof(double) * 3 * nv), *u = malloc(sizeof(double) * N), *v_gpu = malloc(sizeof(double) * N),
@@ -193,6 +218,14 @@ int main(void) {
   for (int i = 0; i < N; i++) err = fmax(err, fabs(v_gpu[i] - v_ref[i])), scale = fmax(scale, fabs(v_ref[i]));
   if (err > 1e-12 * scale) printf("Error: user QFunction on /gpu/cuda/b200 differs from /cpu/self/ref/serial by %e (relative)\n", err / scale);
   fail |= err > 1e-12 * scale;
+  double *s_gpu = malloc(sizeof(double) * 2 * N), *s_ref = malloc(sizeof(double) * 2 * N);
+  Strided("/gpu/cuda/b200", N, u, s_gpu);
+  Strided("/cpu/self/ref/serial", N, u, s_ref);
+  int strided_diff = 0;
+  for (int i = 0; i < 2 * N; i++) strided_diff += s_gpu[i] != s_ref[i];
+  if (strided_diff) printf("Error: strided set/copy on /gpu/cuda/b200 differs in %d entries\n", strided_diff);
+  fail |= strided_diff != 0;
+  free(s_gpu), free(s_ref);
   free(coords), free(u), free(v_gpu), free(v_ref), free(xoff), free(uoff);
   return fail;
 }
