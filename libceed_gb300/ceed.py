@@ -186,8 +186,16 @@ class Vector:
     def ptr(self):
         return _vp(self.data.data_ptr())
 
+    @property
+    def __cuda_array_interface__(self):
+        """The device array, for CuPy, Numba and other consumers of the CUDA array interface (no copy)."""
+        return self.data.__cuda_array_interface__
+
     def set_array(self, array, memtype=MEM_HOST, cmode=COPY_VALUES):
-        """Copy (or, for a device tensor with USE_POINTER, borrow) the values."""
+        """Copy (or, for a device array with USE_POINTER, borrow) the values.  A device array is a torch tensor or any
+        object with __cuda_array_interface__ (CuPy, Numba), taken without a copy as python/ceed_vector.py:73-102 does."""
+        if not isinstance(array, torch.Tensor) and hasattr(array, "__cuda_array_interface__"):
+            array = torch.as_tensor(array, device=self.ceed.device)  # a view of the same device memory
         if isinstance(array, torch.Tensor):
             if cmode == USE_POINTER and array.is_cuda and array.dtype == self.dtype and array.numel() == self.size and array.is_contiguous():
                 self.data = array

@@ -82,6 +82,32 @@ def test_vector_strided_rejects_bad_ranges(ceed):
     assert np.all(x.get_array_read() == 1.0)
 
 
+class _ForeignDeviceArray:
+    """A device array known only through __cuda_array_interface__, as CuPy and Numba arrays present themselves."""
+
+    def __init__(self, t):
+        self._owner = t
+        self.__cuda_array_interface__ = t.__cuda_array_interface__
+
+
+def test_vector_cuda_array_interface(ceed):
+    """Zero-copy device arrays both ways (python/ceed_vector.py:73-102, :159-170): USE_POINTER borrows a foreign
+    array, COPY_VALUES copies it, and the vector exports its own array."""
+    t = torch.arange(10, dtype=torch.float64, device="cuda")
+    v = ceed.Vector(10)
+    v.set_array(_ForeignDeviceArray(t), lc.MEM_DEVICE, lc.USE_POINTER)
+    v.scale(2.0)
+    torch.cuda.synchronize()
+    assert t.cpu().tolist() == [2.0 * i for i in range(10)]
+    assert v.__cuda_array_interface__["data"][0] == t.data_ptr()
+    w = ceed.Vector(10)
+    w.set_array(_ForeignDeviceArray(t), lc.MEM_DEVICE, lc.COPY_VALUES)
+    w.set_value(0.0)
+    torch.cuda.synchronize()
+    assert t.cpu().tolist() == [2.0 * i for i in range(10)]
+    assert np.all(w.get_array_read() == 0.0)
+
+
 def test_empty_vectors(ceed):
     v = ceed.Vector(0)
     v.set_value(1.0)
