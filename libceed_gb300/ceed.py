@@ -9,6 +9,7 @@ CPU fallback: a missing library or an unsupported configuration raises.
 Layouts (published the way CeedElemRestrictionSetELayout does):
   E-vector [comp][elem][node], Q-vector [eval-dim][comp][elem][qpt], qdata [comp][elem][qpt].
 """
+import contextlib
 import ctypes
 import re
 
@@ -176,6 +177,16 @@ class Vector:
         self.dtype = dtype
         self.prec = _prec(dtype)
         self.data = torch.empty(self.size, dtype=dtype, device=ceed.device)
+        self._host = None      # host array handed out by get_array / get_array_write, written back by restore_array
+        self._borrowed = None  # the array given with USE_POINTER, returned by take_array
+
+    def __repr__(self):
+        return f"CeedVector length {self.size} ({self.dtype}) on {self.data.device}"
+
+    def __str__(self):
+        """Like CeedVectorView: the length, then one value per line."""
+        vals = self.get_array_read()
+        return "\n".join([f"CeedVector length {self.size}"] + [f"  {float(x):.14g}" for x in vals])
 
     def __len__(self):
         return self.size
@@ -194,6 +205,8 @@ class Vector:
     def set_array(self, array, memtype=MEM_HOST, cmode=COPY_VALUES):
         """Copy (or, for a device array with USE_POINTER, borrow) the values.  A device array is a torch tensor or any
         object with __cuda_array_interface__ (CuPy, Numba), taken without a copy as python/ceed_vector.py:73-102 does."""
+        given = array
+        self._borrowed = given if cmode == USE_POINTER else None
         if not isinstance(array, torch.Tensor) and hasattr(array, "__cuda_array_interface__"):
             array = torch.as_tensor(array, device=self.ceed.device)  # a view of the same device memory
         if isinstance(array, torch.Tensor):
@@ -207,13 +220,86 @@ class Vector:
                 raise B200Error("CeedVectorSetArray", 2, f"array of {a.size} entries for a vector of {self.size}")
             self.data.copy_(torch.from_numpy(a).to(self.dtype))
 
+    def take_array(self, memtype=MEM_HOST):
+        """CeedVectorTakeArray: return the array given with USE_POINTER and forget it (python/ceed_vector.py:105-125).
+        A host array given with USE_POINTER was copied to the device, so the vector's current values are copied back
+        into it first; a device array was used in place.  The vector holds no valid data afterwards."""
+        given = self._borrowed
+        if given is None:
+            raise B200Error("CeedVectorTakeArray", 5, "no array was set with USE_POINTER")
+        if isinstance(given, np.ndarray):
+            given[...] = self.data.cpu().numpy().reshape(given.shape)
+        else:
+            view = given if isinstance(given, torch.Tensor) else torch.as_tensor(given, device=self.ceed.device)
+            if view.data_ptr() != self.data.data_ptr():  # copied at set_array (another type or layout): copy back
+                view.copy_(self.data.reshape(view.shape))
+        self._borrowed = None
+        self._host = None
+        self.data = torch.empty(self.size, dtype=self.dtype, device=self.ceed.device)
+        return given
+
+    def sync_array(self, memtype=MEM_HOST):
+        """CeedVectorSyncArray: the device array is always current and host arrays are made on request, so there is
+        nothing to move; waits for the work queued on the device array."""
+        if self.data.is_cuda:
+            self.ceed.synchronize()
+
+    def _host_copy(self):
+        h = self.data.cpu().numpy()
+        return h if self.data.is_cuda else h.copy()  # always an array of its own, as after a device-to-host copy
+
     def get_array_read(self, memtype=MEM_HOST):
+        """CeedVectorGetArrayRead: the device tensor, or a host copy of it."""
         if memtype == MEM_DEVICE:
             return self.data
-        return self.data.cpu().numpy()
+        return self._host_copy()
 
     def get_array(self, memtype=MEM_HOST):
-        return self.get_array_read(memtype)
+        """CeedVectorGetArray: read/write access.  MEM_DEVICE gives the device tensor itself; MEM_HOST gives a host
+        array that restore_array() copies back, so host writes reach the vector as with the reference's host view."""
+        if memtype == MEM_DEVICE:
+            return self.data
+        self._host = self._host_copy()
+        return self._host
+
+    def get_array_write(self, memtype=MEM_HOST):
+        """CeedVectorGetArrayWrite: write access; restore_array() publishes the values written."""
+        return self.get_array(memtype)
+
+    def restore_array(self):
+        """CeedVectorRestoreArray: a host array from get_array / get_array_write goes back to the device."""
+        if self._host is not None:
+            self.data.copy_(torch.from_numpy(self._host).to(self.dtype))
+            self._host = None
+
+    def restore_array_read(self):
+        """CeedVectorRestoreArrayRead: read access ends; nothing is written back."""
+
+    @contextlib.contextmanager
+    def array(self, memtype=MEM_HOST):
+        """`with v.array() as a:` read/write access, restored at the end of the block."""
+        a = self.get_array(memtype)
+        try:
+            yield a
+        finally:
+            self.restore_array()
+
+    @contextlib.contextmanager
+    def array_read(self, memtype=MEM_HOST):
+        """`with v.array_read() as a:` read access."""
+        try:
+            yield self.get_array_read(memtype)
+        finally:
+            self.restore_array_read()
+
+    @contextlib.contextmanager
+    def array_write(self, memtype=MEM_HOST):
+        """`with v.array_write() as a:` write access, published at the end of the block."""
+        a = self.get_array_write(memtype)
+        try:
+            yield a
+        finally:
+            self.restore_array()
 
     def set_value(self, value):
         call("b200_vec_set_value", self.ceed._ctx, self.prec, self.size, self.ptr(), float(value))
