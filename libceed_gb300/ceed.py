@@ -77,6 +77,10 @@ class Ceed:
     def get_preferred_memtype(self):
         return MEM_DEVICE
 
+    def scalar_type(self):
+        """numpy name of CeedScalar (python/ceed.py:107-113): double; FP32 vectors are a per-Vector choice here."""
+        return "float64"
+
     def set_deterministic(self, flag=True):
         """CeedSetDeterministic: transposed restrictions and operators use the inverse-offset scatter."""
         self.deterministic = bool(flag)
@@ -346,6 +350,42 @@ class Vector:
         self.data.copy_(other.data.to(self.dtype))
 
 
+class TransposeElemRestriction:
+    """The transpose of a restriction, from E-vectors to L-vectors (python/ceed_elemrestriction.py:459-495)."""
+
+    def __init__(self, elemrestriction):
+        self._elemrestriction = elemrestriction
+
+    def __repr__(self):
+        return f"<Transpose CeedElemRestriction instance at {hex(id(self))}>"
+
+    def apply(self, u, v, request=REQUEST_IMMEDIATE):
+        self._elemrestriction.apply(u, v, tmode=TRANSPOSE, request=request)
+
+
+class TransposeBasis:
+    """The transpose of a basis, from quadrature points to nodes (python/ceed_basis.py:424-460)."""
+
+    def __init__(self, basis):
+        self._basis = basis
+
+    def __repr__(self):
+        return f"<Transpose CeedBasis instance at {hex(id(self))}>"
+
+    def apply(self, nelem, emode, u, v):
+        self._basis.apply(nelem, emode, u, v, tmode=TRANSPOSE)
+
+
+def _multiplicity(offsets, ncomp, compstride, lsize):
+    """E^T (E 1) of an offset restriction (interface/ceed-elemrestriction.c:1722-1737): how many element nodes share
+    each L-vector entry, counted on the host from the offsets."""
+    off = np.asarray(offsets, dtype=np.int64).reshape(-1)
+    mult = np.zeros(lsize)
+    for c in range(ncomp):
+        mult += np.bincount(off + c * compstride, minlength=lsize)[:lsize]
+    return mult
+
+
 class ElemRestriction:
     """Offset element restriction (CeedElemRestrictionCreate); E-vector layout [comp][elem][node]."""
 
@@ -364,6 +404,24 @@ class ElemRestriction:
 
     def get_e_layout(self):
         return (1, self.nelem * self.elemsize, self.elemsize)
+
+    def get_l_layout(self):
+        """Only strided restrictions have an L-vector layout (interface/ceed-elemrestriction.c:385-400)."""
+        raise B200Error("CeedElemRestrictionGetLLayout", 1, "Only strided CeedElemRestriction have strided L-vector layout")
+
+    @property
+    def T(self):
+        return TransposeElemRestriction(self)
+
+    @property
+    def transpose(self):
+        return TransposeElemRestriction(self)
+
+    def get_multiplicity(self):
+        """L-vector of how many element nodes share each entry (CeedElemRestrictionGetMultiplicity)."""
+        mult = Vector(self.ceed, self.lsize)
+        mult.set_array(_multiplicity(self.offsets_host, self.ncomp, self.compstride, self.lsize))
+        return mult
 
     def create_vector(self, dtype=torch.float64):
         return Vector(self.ceed, self.lsize, dtype), Vector(self.ceed, self.nelem * self.elemsize * self.ncomp, dtype)
@@ -410,6 +468,28 @@ class StridedElemRestriction:
     def get_e_layout(self):
         return (1, self.nelem * self.elemsize, self.elemsize)
 
+    def get_l_layout(self):
+        """[node, component, element] strides of the L-vector (CeedElemRestrictionGetLLayout); the backend strides
+        are this backend's E-layout."""
+        return np.array(self.strides, dtype=np.int32)
+
+    @property
+    def T(self):
+        return TransposeElemRestriction(self)
+
+    @property
+    def transpose(self):
+        return TransposeElemRestriction(self)
+
+    def get_multiplicity(self):
+        """Every L-vector entry of a strided restriction belongs to one element node: all ones."""
+        mult = Vector(self.ceed, self.lsize)
+        mult.set_array(np.ones(self.lsize))
+        return mult
+
+    def create_vector(self, dtype=torch.float64):
+        return Vector(self.ceed, self.lsize, dtype), Vector(self.ceed, self.nelem * self.elemsize * self.ncomp, dtype)
+
     def apply(self, u, v, tmode=NOTRANSPOSE, request=REQUEST_IMMEDIATE):
         s = (ctypes.c_int64 * 3)(*self.strides)
         # (node, comp, elem) strides as the reference: index = node*s0 + comp*s1 + elem*s2
@@ -434,6 +514,14 @@ class BasisTensorH1:
         call("b200_basis_create", ceed._ctx, self.dim, self.P1d, self.Q1d, self.ncomp, self.interp1d.ctypes.data_as(ctypes.c_void_p),
              self.grad1d.ctypes.data_as(ctypes.c_void_p), self.qweight1d.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
         self._h = h
+
+    @property
+    def T(self):
+        return TransposeBasis(self)
+
+    @property
+    def transpose(self):
+        return TransposeBasis(self)
 
     def get_num_nodes(self):
         return self.P1d ** self.dim
@@ -497,14 +585,45 @@ class QFunctionContext:
 
     def __init__(self, ceed):
         self.ceed = ceed
-        self.data = None
+        self._bytes = None  # device copy of the context (uint8)
+        self._host = None   # host array handed out by get_data, written back by restore_data
 
     def set_data(self, data, memtype=MEM_HOST, cmode=COPY_VALUES):
         raw = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
-        self.data = torch.from_numpy(raw.copy()).to(self.ceed.device)
+        self._bytes = torch.from_numpy(raw.copy()).to(self.ceed.device)
+        self._host = None
+
+    def get_context_size(self):
+        return 0 if self._bytes is None else int(self._bytes.numel())
+
+    def get_data(self, memtype=MEM_HOST):
+        """Read/write access to the context as CeedScalar (float64) values (python/ceed_qfunctioncontext.py:99-146):
+        the device bytes viewed as doubles, or a host copy that restore_data() writes back."""
+        if self._bytes is None:
+            raise B200Error("CeedQFunctionContextGetData", 5, "the context holds no data")
+        if memtype == MEM_DEVICE:
+            return self._bytes.view(torch.float64)
+        self._host = self._bytes.cpu().numpy().copy().view(np.float64)
+        return self._host
+
+    def restore_data(self):
+        """Publish the host array of get_data() (CeedQFunctionContextRestoreData)."""
+        if self._host is not None:
+            self._bytes.copy_(torch.from_numpy(self._host.view(np.uint8)))
+            self._host = None
+
+    @contextlib.contextmanager
+    def data(self, *shape, memtype=MEM_HOST):
+        """`with ctx.data() as x:` a writable float64 view, optionally reshaped, published at the end of the block
+        (python/ceed_qfunctioncontext.py:159-176)."""
+        x = self.get_data(memtype=memtype)
+        try:
+            yield x.reshape(shape) if shape else x
+        finally:
+            self.restore_data()
 
     def ptr(self):
-        return _vp(self.data.data_ptr()) if self.data is not None else None
+        return _vp(self._bytes.data_ptr()) if self._bytes is not None else None
 
 
 class QFunctionByName:
@@ -552,6 +671,30 @@ class Operator:
         if name not in names:
             raise B200Error("CeedOperatorSetField", 2, f"QFunction {self.qf.name} has no field {name!r}")
         self.fields[name] = _Field(name, rstr, basis, vec)
+
+    def name(self, name):
+        """CeedOperatorSetName (python/ceed_operator.py:112-120)."""
+        self._name = str(name)
+
+    def check(self):
+        """CeedOperatorCheckReady (interface/ceed-operator.c:1450): every field of the QFunction has been set."""
+        missing = [f[0] for f in list(self.qf.inputs) + list(self.qf.outputs) if f[0] not in self.fields]
+        if missing:
+            raise B200Error("CeedOperatorCheckReady", 3, f"fields not set: {', '.join(missing)}")
+
+    def linear_assemble_diagonal(self, d, request=REQUEST_IMMEDIATE):
+        """CeedOperatorLinearAssembleDiagonal: d (an FP64 L-vector) = diag(A), by the diagonal-assembly kernel."""
+        from .solver import assemble_diagonal
+
+        if d.dtype != torch.float64:
+            raise B200Error("CeedOperatorLinearAssembleDiagonal", 4, "the diagonal is assembled into an FP64 vector")
+        assemble_diagonal(self.ceed, self, d)
+
+    def linear_assemble_add_diagonal(self, d, request=REQUEST_IMMEDIATE):
+        """CeedOperatorLinearAssembleAddDiagonal: d += diag(A)."""
+        tmp = Vector(self.ceed, d.size)
+        self.linear_assemble_diagonal(tmp)
+        d.axpy(1.0, tmp)
 
     # ---- the fused path ---------------------------------------------------------------------------------------------
     def _active_input(self):
@@ -734,6 +877,22 @@ class CompositeOperator:
     def apply_add(self, u, v, request=REQUEST_IMMEDIATE):
         for op in self.subs:
             op.apply_add(u, v)
+
+    def name(self, name):
+        self._name = str(name)
+
+    def check(self):
+        for op in self.subs:
+            op.check()
+
+    def linear_assemble_diagonal(self, d, request=REQUEST_IMMEDIATE):
+        """Sum of the sub-operators' diagonals (the interface assembles composites sub-operator by sub-operator)."""
+        d.set_value(0.0)
+        self.linear_assemble_add_diagonal(d)
+
+    def linear_assemble_add_diagonal(self, d, request=REQUEST_IMMEDIATE):
+        for op in self.subs:
+            op.linear_assemble_add_diagonal(d)
 
 
 class _FusedOp:
