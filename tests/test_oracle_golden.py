@@ -157,3 +157,41 @@ def test_linear_fields_energy_identity(n, p):
     s = xyz.sum(axis=1)
     assert abs(s @ pb.apply(s) - 3.0) < 1e-12
     assert abs(xyz[:, 0] @ pb.apply(xyz[:, 1])) < 1e-12
+
+
+@pytest.mark.parametrize("dim", [1, 2, 3])
+@pytest.mark.parametrize("P", [2, 4, 6, 9])
+def test_basis_grad_adjoint(dim, P):
+    """<G^T 1, u> = sum(G u), the reference's tests/t314-basis.c identity (its FP64 tolerance 1e-10), on the oracle's
+    tensor gradient with Gauss points Q = P + 1."""
+    Q = P + 1
+    interp, grad, _, qw = orc.lagrange_1d(P, Q)
+    u = mesh.uniform(314 + P, P ** dim)
+    gu = orc.basis_apply(dim, P, Q, 1, interp, grad, qw, 1, orc.NOTRANSPOSE, orc.EVAL_GRAD, u)
+    gt1 = orc.basis_apply(dim, P, Q, 1, interp, grad, qw, 1, orc.TRANSPOSE, orc.EVAL_GRAD, np.ones(dim * Q ** dim))
+    assert abs(gt1 @ u - gu.sum()) < 1e-10
+
+
+@pytest.mark.parametrize("dim", [1, 3])
+@pytest.mark.parametrize("P", [2, 3, 5, 8])
+def test_basis_interp_polynomial_exact(dim, P):
+    """Interpolating a polynomial of degree P - 1 per direction from the Gauss-Lobatto nodes to the Gauss points is
+    exact (the reference's tests/t311-basis.c, 1D, 100 machine epsilons; 1e-13 here, which also covers 3D)."""
+    from libceed_gb300 import basis1d
+
+    Q = P + 1
+    interp, grad, qref, qw = orc.lagrange_1d(P, Q)
+    nodes, _ = basis1d.lobatto_quadrature(P)
+    c = mesh.uniform(311 + P, dim * P)
+
+    def poly(x, d):  # sum_k c[d, k] x^k, degree P - 1
+        return sum(c[d * P + k] * x ** k for k in range(P))
+
+    def tensor(points):  # values at the tensor grid of `points`, x fastest
+        vals = np.ones(1)
+        for d in range(dim):
+            vals = np.multiply.outer(poly(points, d), vals) if d else poly(points, 0)
+        return np.asarray(vals).reshape(-1)
+
+    got = orc.basis_apply(dim, P, Q, 1, interp, grad, qw, 1, orc.NOTRANSPOSE, orc.EVAL_INTERP, tensor(nodes))
+    assert np.max(np.abs(got - tensor(qref))) < 1e-13
