@@ -117,3 +117,28 @@ def test_diagonal_assembly_plumbing(host_ceed, monkeypatch):
 
 def test_scalar_type():
     assert cm.Ceed.scalar_type(None) == "float64"
+
+
+def test_multiplicity_known_answer(host_ceed):
+    """The reference's tests/t209-elemrestriction.c: 3 elements of 4 nodes sharing one node with each neighbour."""
+    ne = 3
+    ind = np.array([[3 * e + k for k in range(4)] for e in range(ne)], dtype=np.int32).reshape(-1)
+    r = cm.ElemRestriction(host_ceed, ne, 4, 1, 1, 3 * ne + 1, ind)
+    want = [1 + (1 if 0 < i < 3 * ne and i % 3 == 0 else 0) for i in range(3 * ne + 1)]
+    assert r.get_multiplicity().get_array_read().tolist() == want
+
+
+def test_transpose_known_answer_on_oracle():
+    """The reference's tests/t206-elemrestriction.c on the oracle's scatter: 5 two-node elements, 2 components with
+    component stride num_elem + 1; y[i] = i * mult and y[i + ne + 1] = (10 + i) * mult."""
+    ne, P, nc = 5, 2, 2
+    ind = np.array([[e, e + 1] for e in range(ne)], dtype=np.int32).reshape(-1)
+    x = np.zeros(ne * nc * P)
+    for i in range(P):  # node
+        for j in range(nc):  # component
+            for k in range(ne):  # element; the oracle's E-layout is [elem][comp][node]
+                x[i + P * j + P * nc * k] = 10 * j + (2 * k + i + 1) // 2
+    y = orc.rstr_scatter_add(ind, P, nc, ne + 1, x, np.zeros(nc * (ne + 1)))
+    for i in range(ne + 1):
+        mult = 2 if 0 < i < ne else 1
+        assert y[i] == i * mult and y[i + ne + 1] == (10 + i) * mult
