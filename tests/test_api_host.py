@@ -142,3 +142,26 @@ def test_transpose_known_answer_on_oracle():
     for i in range(ne + 1):
         mult = 2 if 0 < i < ne else 1
         assert y[i] == i * mult and y[i + ne + 1] == (10 + i) * mult
+
+
+def test_cg_solve_passes_each_option_to_its_field(monkeypatch):
+    """solver.cg_solve builds b200_cg_opts positionally; every keyword must land in the field of the same meaning."""
+    from libceed_gb300 import solver
+
+    seen = {}
+
+    def call(name, *args):
+        assert name == "b200_cg_solve"
+        seen["opts"] = args[-2]._obj
+        stats = args[-1]._obj
+        stats.iterations, stats.outer, stats.converged, stats.rel_residual = 42, 3, 1, 5e-11
+
+    monkeypatch.setattr(solver, "call", call)
+    vec = types.SimpleNamespace(ptr=lambda: None, size=10, data=types.SimpleNamespace(data_ptr=lambda: 0x1000))
+    op = types.SimpleNamespace(fused=lambda prec: types.SimpleNamespace(h="h"), _kernel_prec=lambda prec: prec)
+    out = solver.cg_solve(types.SimpleNamespace(_ctx=None), op, vec, vec, vec, vec, mixed=True, op32=op, qdata32=vec, rtol=1e-9,
+                          inner_rtol=2e-3, max_it=777, max_outer=11, use_graph=False, check_every=13, jacobi=vec, fused_pdot=False)
+    o = seen["opts"]
+    assert (o.rtol, o.max_it, o.mixed, o.inner_rtol, o.max_outer, o.use_graph, o.check_every, o.jacobi, o.separate_pdot) == (
+        1e-9, 777, 1, 2e-3, 11, 0, 13, 0x1000, 1)
+    assert out["iterations"] == 42 and out["outer"] == 3 and out["converged"] is True and out["rel_residual"] == 5e-11
